@@ -1,0 +1,142 @@
+/*
+ * linac_gb300 -- C ABI of the GB300 (sm_103a) dense RREF / monomial-loader
+ * library.
+ *
+ * Plain pointers and sizes only.  Every function returns an LNC_* status
+ * (0 = success); on failure lnc_last_error() returns a message for the calling
+ * thread.  Matrices are row-major with an explicit leading dimension counted
+ * in elements.  dtype codes: LNC_U32 / LNC_U64 residues mod p, LNC_F64 reals,
+ * LNC_C128 complex (interleaved real, imaginary doubles).
+ *
+ * The reference (GDeLaurentis/linac v1.0.1) exposes Python functions backed by
+ * pycuda, not a C ABI; each entry point below names the reference interface it
+ * replaces.  INTEGRATION.md shows the ctypes binding that the reference-side
+ * Python would use.
+ */
+#ifndef LINAC_GB300_H
+#define LINAC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LNC_OK 0
+#define LNC_ERR_INVALID (-1)   /* bad argument, shape or dtype              */
+#define LNC_ERR_NOT_PRIME (-2) /* modulus is not prime (no inverse exists)  */
+#define LNC_ERR_CUDA (-3)      /* CUDA runtime error (message has details)  */
+#define LNC_ERR_OOM (-4)       /* device allocation failed                  */
+#define LNC_ERR_TIMEOUT (-5)   /* a bounded device-side wait ran out        */
+#define LNC_ERR_ADMISSION (-6) /* request rejected by memory admission      */
+#define LNC_ERR_NO_DEVICE (-7) /* no CUDA device                            */
+#define LNC_ERR_UNSUPPORTED (-8) /* valid request this build cannot serve   */
+
+/* ---- element types ------------------------------------------------------ */
+#define LNC_U32 1
+#define LNC_U64 2
+#define LNC_F64 3
+#define LNC_C128 4
+
+/* ---- flags for the RREF entry points ----------------------------------- */
+#define LNC_FLAG_NONE 0
+#define LNC_FLAG_NO_SCALING 1   /* float path: skip the row pre-scaling     */
+#define LNC_FLAG_SIMT_TRAILING 2 /* force the SIMT trailing update (tests)  */
+
+/* ---- library / device ---------------------------------------------------- */
+/* Version string of the library. */
+const char* lnc_version(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char* lnc_last_error(void);
+/* Number of visible CUDA devices (0 when none).  Replaces the pycuda probe
+ * behind CUDA_FOUND (linac/_optional.py:11-23). */
+int lnc_device_count(void);
+/* Select the device used by this thread's subsequent calls. */
+int lnc_set_device(int device);
+/* SM count, free and total device memory of the current device. */
+int lnc_device_info(int* sms, size_t* free_bytes, size_t* total_bytes);
+/* Number of kernels this library has launched (monotonic counter). */
+int64_t lnc_launch_count(void);
+
+/* ---- memory, streams, events (thin CUDA runtime wrappers, so that callers
+ *      need no CUDA bindings of their own) ------------------------------------ */
+int lnc_malloc(void** dev_ptr, size_t bytes);
+int lnc_free(void* dev_ptr);
+int lnc_malloc_host(void** host_ptr, size_t bytes); /* pinned host memory */
+int lnc_free_host(void* host_ptr);
+int lnc_memcpy_h2d(void* dst, const void* src, size_t bytes, void* stream);
+int lnc_memcpy_d2h(void* dst, const void* src, size_t bytes, void* stream);
+int lnc_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream);
+int lnc_memset(void* dev_ptr, int value, size_t bytes, void* stream);
+int lnc_stream_create(void** stream);
+int lnc_stream_destroy(void* stream);
+int lnc_stream_synchronize(void* stream);
+int lnc_device_synchronize(void);
+int lnc_event_create(void** event);
+int lnc_event_destroy(void* event);
+int lnc_event_record(void* event, void* stream);
+int lnc_event_elapsed_ms(void* start, void* stop, float* ms);
+/* Read (and clear) the device-side error word that bounded waits set; returns
+ * the status it held (LNC_OK when none).  Synchronises the device. */
+int lnc_device_status(void);
+
+/* ---- kernel timing (CUDA events on the launching stream) ------------------ */
+/* kernel classes: 0 panel, 1 trailing update, 2 loader, 3 gather, 4 batch */
+int lnc_kernel_timing_enable(int enable);
+int lnc_kernel_timing_reset(void);
+/* Total launches and summed event time (ms) of one class since the reset;
+ * synchronises the events it reads. */
+int lnc_kernel_timing_read(int kernel_class, int64_t* launches, double* total_ms);
+
+/* ---- RREF ------------------------------------------------------------------ */
+/*
+ * Reduced row-echelon form of a host matrix: reads host_in (m x n, leading
+ * dimension ld_in elements), writes the RREF to host_out (ld_out; may equal
+ * host_in).  p is the field characteristic (ignored for LNC_F64 / LNC_C128,
+ * where `tol` is the head threshold and the rows are pre-scaled by their
+ * largest |a| unless LNC_FLAG_NO_SCALING).  Optional outputs: pivot_cols
+ * (min(m,n) entries, -1 past the rank) and *rank.  Synchronous.
+ * Replaces cuda_row_reduce (linac/pycuda_row_reduce.py:18-151): the H2D copy
+ * (:71-79), the per-column launch loop (:94-131) and the D2H copy (:141-149).
+ */
+int lnc_rref_host(int dtype, int64_t m, int64_t n, uint64_t p, double tol, const void* host_in,
+                  int64_t ld_in, void* host_out, int64_t ld_out, int64_t* pivot_cols, int64_t* rank,
+                  int flags);
+
+/*
+ * Device-resident RREF on `stream`.  `dev_work` (m x n, ld_work) holds the
+ * input and is destroyed; the RREF is written to `dev_out` (ld_out), which may
+ * equal dev_work.  dev_pivot_cols (min(m,n) int64) and dev_rank (one int64)
+ * are optional device outputs.  Asynchronous: errors of bounded device waits
+ * surface through lnc_device_status().
+ * Replaces the device half of cuda_row_reduce (linac/pycuda_row_reduce.py:81-131)
+ * and its kernels (linac/row_reduce.cu:117-430).
+ */
+int lnc_rref_device(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* dev_work,
+                    int64_t ld_work, void* dev_out, int64_t ld_out, int64_t* dev_pivot_cols,
+                    int64_t* dev_rank, void* stream, int flags);
+
+/* ---- monomial loader --------------------------------------------------------- */
+/*
+ * out[r, c] = prod_{t<degree} bases[r, lindices[c, t]] (mod p for LNC_U32 /
+ * LNC_U64; plain products for LNC_F64 / LNC_C128), folded left to right; a
+ * single factor is copied as is.  bases is n_rows x basis_len, lindices is
+ * n_cols x degree (uint32), out is n_rows x n_cols (ld_out).
+ * Replaces cuda_load_matrix (linac/pycuda_matrix_loader.py:27-124) and its
+ * kernel LoadMatrix (linac/matrix_loader.cu:88-112).
+ */
+int lnc_load_matrix_host(int dtype, int64_t n_rows, int64_t n_cols, int64_t basis_len,
+                         int64_t degree, uint64_t p, const void* host_bases,
+                         const uint32_t* host_lindices, void* host_out);
+int lnc_load_matrix_device(int dtype, int64_t n_rows, int64_t n_cols, int64_t basis_len,
+                           int64_t degree, uint64_t p, const void* dev_bases,
+                           const uint32_t* dev_lindices, void* dev_out, int64_t ld_out,
+                           void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LINAC_GB300_H */

@@ -1,0 +1,457 @@
+// C ABI of liblinac_gb300 (declared in include/linac_gb300.h) and the shared
+// host-side helpers: error messages, launch counting, kernel timing, device
+// properties and the per-thread library stream.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "rref_internal.cuh"
+
+namespace lnc {
+
+static thread_local std::string t_last_error;
+static std::atomic<int64_t> g_launches{0};
+
+void set_error(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_last_error = buf;
+}
+
+int cuda_status(cudaError_t e, const char* what) {
+    set_error("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    if (e == cudaErrorMemoryAllocation) return LNC_ERR_OOM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return LNC_ERR_NO_DEVICE;
+    return LNC_ERR_CUDA;
+}
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// ---- kernel timing ---------------------------------------------------------
+static std::mutex g_timing_mu;
+static bool g_timing_enabled = false;
+static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_timing_pending[KC_COUNT];
+static std::vector<cudaEvent_t> g_event_pool;
+static int64_t g_timing_launches[KC_COUNT];
+static double g_timing_ms[KC_COUNT];
+
+static cudaEvent_t pool_event() {
+    if (!g_event_pool.empty()) {
+        cudaEvent_t e = g_event_pool.back();
+        g_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+ScopedKernelTimer::ScopedKernelTimer(int kc, cudaStream_t s) : kclass(kc), stream(s) {
+    std::lock_guard<std::mutex> g(g_timing_mu);
+    if (!g_timing_enabled) return;
+    start = pool_event();
+    stop = pool_event();
+    if (start) cudaEventRecord(start, stream);
+}
+
+ScopedKernelTimer::~ScopedKernelTimer() {
+    if (!start) return;
+    std::lock_guard<std::mutex> g(g_timing_mu);
+    cudaEventRecord(stop, stream);
+    g_timing_pending[kclass].push_back({start, stop});
+}
+
+static void timing_drain_locked() {
+    for (int k = 0; k < KC_COUNT; ++k) {
+        for (auto& pr : g_timing_pending[k]) {
+            cudaEventSynchronize(pr.second);
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) {
+                g_timing_ms[k] += ms;
+                g_timing_launches[k] += 1;
+            }
+            g_event_pool.push_back(pr.first);
+            g_event_pool.push_back(pr.second);
+        }
+        g_timing_pending[k].clear();
+    }
+}
+
+// ---- device properties -----------------------------------------------------
+static std::mutex g_dev_mu;
+static DeviceInfo g_dev_cache[64];
+
+int device_info(DeviceInfo* out) {
+    int dev = 0;
+    LNC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) { set_error("device index out of range"); return LNC_ERR_INVALID; }
+    std::lock_guard<std::mutex> g(g_dev_mu);
+    DeviceInfo& d = g_dev_cache[dev];
+    if (d.device != dev) {
+        cudaDeviceProp prop;
+        LNC_CUDA(cudaGetDeviceProperties(&prop, dev));
+        d.sms = prop.multiProcessorCount;
+        d.smem_optin = (int)prop.sharedMemPerBlockOptin;
+        d.cc_major = prop.major;
+        d.cc_minor = prop.minor;
+        int coop = 0;
+        LNC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        d.coop = coop != 0;
+        // keep freed stream-ordered allocations cached in the pool
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        d.device = dev;
+    }
+    *out = d;
+    return LNC_OK;
+}
+
+// Per-thread library stream (non-blocking), created on first use per device.
+static thread_local cudaStream_t t_streams[64] = {nullptr};
+static int library_stream(cudaStream_t* s) {
+    int dev = 0;
+    LNC_CUDA(cudaGetDevice(&dev));
+    if (!t_streams[dev]) LNC_CUDA(cudaStreamCreateWithFlags(&t_streams[dev], cudaStreamNonBlocking));
+    *s = t_streams[dev];
+    return LNC_OK;
+}
+
+// ---- modulus validation ----------------------------------------------------
+static uint64_t mulmod_u64(uint64_t a, uint64_t b, uint64_t m) {
+    return (uint64_t)(((unsigned __int128)a * b) % m);
+}
+static uint64_t powmod_u64(uint64_t a, uint64_t e, uint64_t m) {
+    uint64_t r = 1 % m;
+    a %= m;
+    while (e) {
+        if (e & 1) r = mulmod_u64(r, a, m);
+        a = mulmod_u64(a, a, m);
+        e >>= 1;
+    }
+    return r;
+}
+bool is_prime_u64(uint64_t n) {
+    if (n < 2) return false;
+    static const uint64_t bases[] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37};
+    for (uint64_t q : bases) {
+        if (n % q == 0) return n == q;
+    }
+    uint64_t d = n - 1;
+    int s = 0;
+    while ((d & 1) == 0) { d >>= 1; ++s; }
+    for (uint64_t a : bases) {
+        uint64_t x = powmod_u64(a, d, n);
+        if (x == 1 || x == n - 1) continue;
+        bool comp = true;
+        for (int i = 1; i < s; ++i) {
+            x = mulmod_u64(x, x, n);
+            if (x == n - 1) { comp = false; break; }
+        }
+        if (comp) return false;
+    }
+    return true;
+}
+
+size_t dtype_size(int dtype) {
+    switch (dtype) {
+        case LNC_U32: return 4;
+        case LNC_U64: return 8;
+        case LNC_F64: return 8;
+        case LNC_C128: return 16;
+        default: return 0;
+    }
+}
+
+int validate_rref_args(int dtype, int64_t m, int64_t n, uint64_t p, int64_t ld) {
+    if (dtype_size(dtype) == 0) { set_error("unknown dtype %d", dtype); return LNC_ERR_INVALID; }
+    if (m < 0 || n < 0) { set_error("negative shape (%lld, %lld)", (long long)m, (long long)n); return LNC_ERR_INVALID; }
+    if (ld < n) { set_error("leading dimension %lld < n = %lld", (long long)ld, (long long)n); return LNC_ERR_INVALID; }
+    if (m > INT32_MAX) { set_error("too many rows (%lld)", (long long)m); return LNC_ERR_UNSUPPORTED; }
+    if (dtype == LNC_U32 || dtype == LNC_U64) {
+        if (dtype == LNC_U32 && p > 0xFFFFFFFFull) { set_error("p = %llu does not fit 32-bit residues", (unsigned long long)p); return LNC_ERR_INVALID; }
+        if (!is_prime_u64(p)) {
+            set_error("Inverse mod %llu does not exist in general. Are you sure %llu is prime?",
+                      (unsigned long long)p, (unsigned long long)p);
+            return LNC_ERR_NOT_PRIME;
+        }
+    }
+    return LNC_OK;
+}
+
+int load_matrix_dispatch(int dtype, int64_t n_rows, int64_t n_cols, int64_t basis_len, int64_t degree,
+                         uint64_t p, const void* bases, const uint32_t* lind, void* out, int64_t ldo,
+                         cudaStream_t s);
+
+}  // namespace lnc
+
+using namespace lnc;
+
+extern "C" {
+
+const char* lnc_version(void) { return "linac_gb300 0.1.0 (sm_103a)"; }
+
+const char* lnc_last_error(void) { return t_last_error.c_str(); }
+
+int lnc_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int lnc_set_device(int device) {
+    LNC_CUDA(cudaSetDevice(device));
+    return LNC_OK;
+}
+
+int lnc_device_info(int* sms, size_t* free_bytes, size_t* total_bytes) {
+    DeviceInfo di;
+    int rc = device_info(&di);
+    if (rc) return rc;
+    if (sms) *sms = di.sms;
+    size_t f = 0, t = 0;
+    LNC_CUDA(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return LNC_OK;
+}
+
+int64_t lnc_launch_count(void) { return g_launches.load(); }
+
+int lnc_malloc(void** p, size_t bytes) {
+    if (!p) return LNC_ERR_INVALID;
+    *p = nullptr;
+    if (bytes == 0) return LNC_OK;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+        return LNC_ERR_OOM;
+    }
+    return LNC_OK;
+}
+int lnc_free(void* p) { LNC_CUDA(cudaFree(p)); return LNC_OK; }
+int lnc_malloc_host(void** p, size_t bytes) {
+    if (!p) return LNC_ERR_INVALID;
+    *p = nullptr;
+    if (bytes == 0) return LNC_OK;
+    cudaError_t e = cudaMallocHost(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cudaMallocHost(%zu): %s", bytes, cudaGetErrorString(e));
+        return LNC_ERR_OOM;
+    }
+    return LNC_OK;
+}
+int lnc_free_host(void* p) { LNC_CUDA(cudaFreeHost(p)); return LNC_OK; }
+int lnc_memcpy_h2d(void* dst, const void* src, size_t bytes, void* stream) {
+    LNC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    return LNC_OK;
+}
+int lnc_memcpy_d2h(void* dst, const void* src, size_t bytes, void* stream) {
+    LNC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    return LNC_OK;
+}
+int lnc_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream) {
+    LNC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    return LNC_OK;
+}
+int lnc_memset(void* p, int value, size_t bytes, void* stream) {
+    LNC_CUDA(cudaMemsetAsync(p, value, bytes, (cudaStream_t)stream));
+    return LNC_OK;
+}
+int lnc_stream_create(void** s) {
+    cudaStream_t st;
+    LNC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    *s = (void*)st;
+    return LNC_OK;
+}
+int lnc_stream_destroy(void* s) { LNC_CUDA(cudaStreamDestroy((cudaStream_t)s)); return LNC_OK; }
+int lnc_stream_synchronize(void* s) { LNC_CUDA(cudaStreamSynchronize((cudaStream_t)s)); return LNC_OK; }
+int lnc_device_synchronize(void) { LNC_CUDA(cudaDeviceSynchronize()); return LNC_OK; }
+int lnc_event_create(void** e) {
+    cudaEvent_t ev;
+    LNC_CUDA(cudaEventCreate(&ev));
+    *e = (void*)ev;
+    return LNC_OK;
+}
+int lnc_event_destroy(void* e) { LNC_CUDA(cudaEventDestroy((cudaEvent_t)e)); return LNC_OK; }
+int lnc_event_record(void* e, void* s) { LNC_CUDA(cudaEventRecord((cudaEvent_t)e, (cudaStream_t)s)); return LNC_OK; }
+int lnc_event_elapsed_ms(void* a, void* b, float* ms) {
+    LNC_CUDA(cudaEventSynchronize((cudaEvent_t)b));
+    LNC_CUDA(cudaEventElapsedTime(ms, (cudaEvent_t)a, (cudaEvent_t)b));
+    return LNC_OK;
+}
+
+int lnc_device_status(void) {
+    LNC_CUDA(cudaDeviceSynchronize());
+    int st = 0;
+    int rc = rref_read_and_clear_status(&st);
+    if (rc) return rc;
+    if (st != 0) {
+        set_error("a bounded device-side wait timed out (status %d)", st);
+        return st;
+    }
+    return LNC_OK;
+}
+
+int lnc_kernel_timing_enable(int enable) {
+    std::lock_guard<std::mutex> g(g_timing_mu);
+    g_timing_enabled = enable != 0;
+    return LNC_OK;
+}
+
+int lnc_kernel_timing_reset(void) {
+    std::lock_guard<std::mutex> g(g_timing_mu);
+    timing_drain_locked();
+    for (int k = 0; k < KC_COUNT; ++k) { g_timing_ms[k] = 0.0; g_timing_launches[k] = 0; }
+    return LNC_OK;
+}
+
+int lnc_kernel_timing_read(int kc, int64_t* launches, double* total_ms) {
+    if (kc < 0 || kc >= KC_COUNT) { set_error("unknown kernel class %d", kc); return LNC_ERR_INVALID; }
+    std::lock_guard<std::mutex> g(g_timing_mu);
+    timing_drain_locked();
+    if (launches) *launches = g_timing_launches[kc];
+    if (total_ms) *total_ms = g_timing_ms[kc];
+    return LNC_OK;
+}
+
+int lnc_rref_device(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* work, int64_t ldw,
+                    void* out, int64_t ldo, int64_t* dev_piv, int64_t* dev_rank, void* stream, int flags) {
+    int rc = validate_rref_args(dtype, m, n, p, ldw);
+    if (rc) return rc;
+    if (ldo < n) { set_error("output leading dimension %lld < n", (long long)ldo); return LNC_ERR_INVALID; }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (m == 0 || n == 0) {
+        if (dev_rank) LNC_CUDA(cudaMemsetAsync(dev_rank, 0, sizeof(int64_t), s));
+        if (dev_piv && std::min(m, n) > 0) LNC_CUDA(cudaMemsetAsync(dev_piv, 0xff, sizeof(int64_t) * std::min(m, n), s));
+        return LNC_OK;
+    }
+    return rref_device_dispatch(dtype, m, n, p, tol, work, ldw, out, ldo, dev_piv, dev_rank, s, flags);
+}
+
+int lnc_rref_host(int dtype, int64_t m, int64_t n, uint64_t p, double tol, const void* host_in,
+                  int64_t ld, void* host_out, int64_t ld_out, int64_t* piv, int64_t* rank, int flags) {
+    int rc = validate_rref_args(dtype, m, n, p, ld);
+    if (rc) return rc;
+    if (ld_out < n) { set_error("output leading dimension %lld < n", (long long)ld_out); return LNC_ERR_INVALID; }
+    const int64_t kmax = std::min(m, n);
+    if (m == 0 || n == 0) {
+        if (rank) *rank = 0;
+        return LNC_OK;
+    }
+    cudaStream_t s;
+    rc = library_stream(&s);
+    if (rc) return rc;
+    const size_t elt = dtype_size(dtype);
+    const size_t bytes = elt * (size_t)m * (size_t)n;
+    void *dwork = nullptr, *dout = nullptr, *dsmall = nullptr;
+    cudaError_t e = cudaMallocAsync(&dwork, bytes, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dout, bytes, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dsmall, sizeof(int64_t) * (size_t)(kmax + 1), s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (dwork) cudaFreeAsync(dwork, s);
+        if (dout) cudaFreeAsync(dout, s);
+        set_error("device allocation for a %lld x %lld matrix failed: %s", (long long)m, (long long)n,
+                  cudaGetErrorString(e));
+        return LNC_ERR_OOM;
+    }
+    int64_t* dpiv = (int64_t*)dsmall;
+    int64_t* drank = dpiv + kmax;
+    e = cudaMemcpy2DAsync(dwork, elt * n, host_in, elt * ld, elt * n, m, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) rc = cuda_status(e, "host-to-device copy");
+    if (!rc) rc = rref_device_dispatch(dtype, m, n, p, tol, dwork, n, dout, n, dpiv, drank, s, flags);
+    if (!rc) {
+        e = cudaMemcpy2DAsync(host_out, elt * ld_out, dout, elt * n, elt * n, m, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) rc = cuda_status(e, "device-to-host copy");
+    }
+    std::vector<int64_t> small((size_t)kmax + 1);
+    if (!rc) {
+        e = cudaMemcpyAsync(small.data(), dsmall, sizeof(int64_t) * (size_t)(kmax + 1), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) rc = cuda_status(e, "device-to-host copy");
+    }
+    cudaFreeAsync(dwork, s);
+    cudaFreeAsync(dout, s);
+    cudaFreeAsync(dsmall, s);
+    e = cudaStreamSynchronize(s);
+    if (!rc && e != cudaSuccess) rc = cuda_status(e, "rref");
+    if (!rc) {
+        int st = 0;
+        rc = rref_read_and_clear_status(&st);
+        if (!rc && st != 0) {
+            set_error("a bounded device-side wait timed out during the RREF (status %d)", st);
+            rc = st;
+        }
+    }
+    if (!rc) {
+        if (piv) memcpy(piv, small.data(), sizeof(int64_t) * (size_t)kmax);
+        if (rank) *rank = small[(size_t)kmax];
+    }
+    return rc;
+}
+
+int lnc_load_matrix_device(int dtype, int64_t n_rows, int64_t n_cols, int64_t basis_len, int64_t degree,
+                           uint64_t p, const void* bases, const uint32_t* lind, void* out, int64_t ldo,
+                           void* stream) {
+    if (dtype_size(dtype) == 0) { set_error("unknown dtype %d", dtype); return LNC_ERR_INVALID; }
+    if (n_rows < 0 || n_cols < 0 || ldo < n_cols) { set_error("loader: bad shape"); return LNC_ERR_INVALID; }
+    return load_matrix_dispatch(dtype, n_rows, n_cols, basis_len, degree, p, bases, lind, out, ldo,
+                                (cudaStream_t)stream);
+}
+
+int lnc_load_matrix_host(int dtype, int64_t n_rows, int64_t n_cols, int64_t basis_len, int64_t degree,
+                         uint64_t p, const void* hbases, const uint32_t* hlind, void* hout) {
+    const size_t elt = dtype_size(dtype);
+    if (elt == 0) { set_error("unknown dtype %d", dtype); return LNC_ERR_INVALID; }
+    if (n_rows < 0 || n_cols < 0 || basis_len < 0 || degree < 0) { set_error("loader: bad shape"); return LNC_ERR_INVALID; }
+    if (n_rows == 0 || n_cols == 0) return LNC_OK;
+    cudaStream_t s;
+    int rc = library_stream(&s);
+    if (rc) return rc;
+    const size_t bb = elt * (size_t)n_rows * (size_t)basis_len;
+    const size_t lb = sizeof(uint32_t) * (size_t)n_cols * (size_t)degree;
+    const size_t ob = elt * (size_t)n_rows * (size_t)n_cols;
+    void *db = nullptr, *dl = nullptr, *dout = nullptr;
+    cudaError_t e = cudaMallocAsync(&db, bb ? bb : 16, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dl, lb ? lb : 16, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dout, ob, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (db) cudaFreeAsync(db, s);
+        if (dl) cudaFreeAsync(dl, s);
+        set_error("loader: device allocation failed: %s", cudaGetErrorString(e));
+        return LNC_ERR_OOM;
+    }
+    if (bb) e = cudaMemcpyAsync(db, hbases, bb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && lb) e = cudaMemcpyAsync(dl, hlind, lb, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) rc = cuda_status(e, "loader host-to-device copy");
+    if (!rc) rc = load_matrix_dispatch(dtype, n_rows, n_cols, basis_len, degree, p, db, (const uint32_t*)dl, dout,
+                                       n_cols, s);
+    if (!rc) {
+        e = cudaMemcpyAsync(hout, dout, ob, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) rc = cuda_status(e, "loader device-to-host copy");
+    }
+    cudaFreeAsync(db, s);
+    cudaFreeAsync(dl, s);
+    cudaFreeAsync(dout, s);
+    e = cudaStreamSynchronize(s);
+    if (!rc && e != cudaSuccess) rc = cuda_status(e, "loader");
+    return rc;
+}
+
+}  // extern "C"

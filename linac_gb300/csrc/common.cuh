@@ -1,0 +1,69 @@
+// Shared definitions for the linac_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "linac_gb300.h"
+
+namespace lnc {
+
+// ---------------------------------------------------------------------------
+// error plumbing: every entry point returns an LNC_* status and leaves a
+// message retrievable through lnc_last_error().
+// ---------------------------------------------------------------------------
+void set_error(const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* what);
+
+#define LNC_CUDA(call)                                                        \
+    do {                                                                      \
+        cudaError_t _e = (call);                                              \
+        if (_e != cudaSuccess) return ::lnc::cuda_status(_e, #call);          \
+    } while (0)
+
+#define LNC_CHECK_LAUNCH(name)                                                \
+    do {                                                                      \
+        cudaError_t _e = cudaGetLastError();                                  \
+        if (_e != cudaSuccess) return ::lnc::cuda_status(_e, name);           \
+        ::lnc::count_launch();                                                \
+    } while (0)
+
+void count_launch();
+
+// Kernel classes whose launches can be timed with CUDA events (see
+// lnc_kernel_timing_*); the dominant kernel of each path has its own class.
+enum KernelClass : int {
+    KC_PANEL = 0,
+    KC_TRAILING = 1,
+    KC_LOADER = 2,
+    KC_GATHER = 3,
+    KC_BATCH = 4,
+    KC_COUNT = 5
+};
+
+struct ScopedKernelTimer {
+    ScopedKernelTimer(int kclass, cudaStream_t s);
+    ~ScopedKernelTimer();
+    int kclass;
+    cudaStream_t stream;
+    cudaEvent_t start = nullptr, stop = nullptr;
+};
+
+// Per-device properties cached at first use.
+struct DeviceInfo {
+    int device = -1;
+    int sms = 0;
+    int smem_optin = 0;      // max dynamic shared memory per block (bytes)
+    int cc_major = 0, cc_minor = 0;
+    bool coop = false;
+};
+int device_info(DeviceInfo* out);
+
+size_t dtype_size(int dtype);
+bool is_prime_u64(uint64_t n);
+
+constexpr int kMaxPanel = 128;           // widest panel (columns)
+constexpr int kPanelThreads = 256;
+
+}  // namespace lnc

@@ -1,0 +1,698 @@
+// Dense reduced row-echelon form on one GPU: blocked right-looking
+// Gauss-Jordan with a cooperative panel kernel and a trailing update.
+//
+// The reference (linac/pycuda_row_reduce.py:94-131 driving
+// linac/row_reduce.cu:273-430) runs an unblocked loop from Python, 6-7 kernel
+// launches per column, each column touching the whole m x (n - j) trailing
+// matrix.  This driver processes `b` columns per panel:
+//
+//  1. panel_kernel (cooperative, one CTA per SM, panel rows held in shared
+//     memory): for each panel column, every CTA proposes its best eligible
+//     row (largest residue / |a|, as in row_reduce.cu:287-393), one bounded
+//     grid barrier exchanges the proposals, and every CTA eliminates its own
+//     rows with the normalised winner (row_reduce.cu:117-196).  Eliminated
+//     pivot columns keep the Gauss-Jordan transform in place ("E"), so that
+//     after the panel   A[:, T] <- A[:, T] (pivot rows zeroed) + E * A[P, T]
+//     applies the whole panel to the trailing columns T in one contraction.
+//  2. gather_pivot_rows: copies the k pivot rows' trailing part to a dense
+//     operand and zeroes them in A.
+//  3. trailing update: the contraction above (tensor-core limb GEMM for
+//     32-bit residues, see trailing_tc.cu; a SIMT kernel here for the other
+//     fields and as the reference implementation for tests).
+//  4. gather_rref_rows: rows are never swapped in memory; pivot rows are
+//     tracked in a list and gathered into RREF order once at the end.
+//
+// The RREF over a field is unique, so the pivot order does not change the
+// F_p result; it is bit-identical to linac's CPU row_reduce.
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "field.cuh"
+#include "sync.cuh"
+#include "rref_internal.cuh"
+
+namespace lnc {
+
+__device__ int g_rref_status = 0;
+
+int rref_read_and_clear_status(int* status) {
+    int v = 0, zero = 0;
+    LNC_CUDA(cudaMemcpyFromSymbol(&v, g_rref_status, sizeof(int)));
+    LNC_CUDA(cudaMemcpyToSymbol(g_rref_status, &zero, sizeof(int)));
+    *status = v;
+    return LNC_OK;
+}
+
+int* rref_status_symbol_address() {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_rref_status) != cudaSuccess) return nullptr;
+    return (int*)p;
+}
+
+// ----------------------------------------------------------------------------
+// key helpers
+// ----------------------------------------------------------------------------
+template <class F> struct KeyNone;
+template <> struct KeyNone<FieldU32> { static __device__ __forceinline__ uint64_t v() { return 0ull; } };
+template <> struct KeyNone<FieldU64> { static __device__ __forceinline__ uint64_t v() { return 0ull; } };
+template <> struct KeyNone<FieldF64> { static __device__ __forceinline__ double v() { return -1.0; } };
+template <> struct KeyNone<FieldC128> { static __device__ __forceinline__ double v() { return -1.0; } };
+
+template <class K>
+__device__ __forceinline__ bool better(K ka, int64_t ra, K kb, int64_t rb) {
+    return ka > kb || (ka == kb && ra < rb);
+}
+
+template <class T>
+__device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
+template <>
+__device__ __forceinline__ c128 ldcg<c128>(const c128* p) {
+    double2 v = __ldcg((const double2*)p);
+    c128 r; r.x = v.x; r.y = v.y; return r;
+}
+
+// ----------------------------------------------------------------------------
+// 0. input preparation
+// ----------------------------------------------------------------------------
+template <class F>
+__global__ void reduce_input_kernel(F f, typename F::T* A, int64_t lda, int64_t m, int64_t n) {
+    for (int64_t r = blockIdx.y; r < m; r += gridDim.y) {
+        typename F::T* row = A + r * lda;
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+             c += (int64_t)gridDim.x * blockDim.x)
+            row[c] = f.reduce_input(row[c]);
+    }
+}
+
+// Row pre-scaling of the float path (linac/row_reduce.cu:201-270): each row
+// divided by its largest |a|.  A zero row is left as is (the reference would
+// divide by zero and fill the row with NaN).
+template <class F>
+__global__ void row_scale_kernel(F f, typename F::T* A, int64_t lda, int64_t m, int64_t n) {
+    __shared__ double s_part[32];
+    for (int64_t r = blockIdx.x; r < m; r += gridDim.x) {
+        typename F::T* row = A + r * lda;
+        double mx = 0.0;
+        for (int64_t c = threadIdx.x; c < n; c += blockDim.x) mx = fmax(mx, (double)f.key(row[c]));
+        for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = mx;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double v = threadIdx.x < (blockDim.x >> 5) ? s_part[threadIdx.x] : 0.0;
+            for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+            if (threadIdx.x == 0) s_part[0] = v;
+        }
+        __syncthreads();
+        double s = s_part[0];
+        __syncthreads();
+        if (s > 0.0) {
+            for (int64_t c = threadIdx.x; c < n; c += blockDim.x) row[c] = scale_real(row[c], s);
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------
+// 1. panel kernel
+// ----------------------------------------------------------------------------
+template <class F>
+__global__ void __launch_bounds__(kPanelThreads, 1) panel_kernel(PanelArgs<F> a) {
+    using T = typename F::T;
+    using Key = typename F::Key;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const F f = a.f;
+    const int G = gridDim.x;
+    const int bw = a.bw;
+    const int RP = a.rows_per_cta;
+    const int64_t r0 = (int64_t)blockIdx.x * RP;
+    const int64_t r1 = min(a.m, r0 + RP);
+    const int R = (int)max((int64_t)0, r1 - r0);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int NW = kPanelThreads / 32;
+
+    T* tile = (T*)smem_raw;                // [RP][bw]
+    T* prow = tile + (size_t)RP * bw;      // [bw]
+    T* fcol = prow + bw;                   // [RP]
+    int* ispiv = (int*)(fcol + RP);        // [bw]
+    uint8_t* used = (uint8_t*)(ispiv + bw);  // [RP]
+
+    __shared__ int64_t s_prows[kMaxPanel];
+    __shared__ int s_pcols[kMaxPanel];
+    __shared__ Key s_wkey[NW];
+    __shared__ int64_t s_wrow[NW];
+    __shared__ int s_wblk[NW];
+    __shared__ int64_t s_cand_row;
+    __shared__ int64_t s_win_row;
+    __shared__ int s_win_blk;
+    __shared__ int s_win_ok;
+    __shared__ T s_inv;
+
+    if (ld_volatile_i32(a.bar.err) != 0) return;
+    const int64_t rank0 = *a.rank;
+
+    for (int r = warp; r < R; r += NW) {
+        const T* src = a.A + (r0 + r) * a.lda + a.j0;
+        for (int c = lane; c < bw; c += 32) tile[(size_t)r * bw + c] = src[c];
+        if (lane == 0) used[r] = a.row_used[r0 + r];
+    }
+    for (int c = threadIdx.x; c < bw; c += blockDim.x) ispiv[c] = -1;
+    __syncthreads();
+
+    int k = 0;
+    for (int c = 0; c < bw; ++c) {
+        if (rank0 + k >= a.m) break;  // every row is a pivot row already
+        const int par = c & 1;
+        // -- local proposal: best eligible row of this CTA for column c
+        Key bk = KeyNone<F>::v();
+        int64_t br = INT64_MAX;
+        for (int r = threadIdx.x; r < R; r += blockDim.x) {
+            if (!used[r]) {
+                Key kk = f.key(tile[(size_t)r * bw + c]);
+                if (better(kk, r0 + r, bk, br)) { bk = kk; br = r0 + r; }
+            }
+        }
+        for (int o = 16; o; o >>= 1) {
+            Key ok = __shfl_down_sync(0xffffffffu, bk, o);
+            int64_t orow = __shfl_down_sync(0xffffffffu, br, o);
+            if (better(ok, orow, bk, br)) { bk = ok; br = orow; }
+        }
+        if (lane == 0) { s_wkey[warp] = bk; s_wrow[warp] = br; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < NW; ++w)
+                if (better(s_wkey[w], s_wrow[w], bk, br)) { bk = s_wkey[w]; br = s_wrow[w]; }
+            a.cand_key[par * G + blockIdx.x] = bk;
+            a.cand_row[par * G + blockIdx.x] = br;
+            s_cand_row = br;
+        }
+        __syncthreads();
+        if (s_cand_row != INT64_MAX) {
+            const int rl = (int)(s_cand_row - r0);
+            T* dst = a.cand_vals + ((size_t)par * G + blockIdx.x) * a.b;
+            for (int cc = threadIdx.x; cc < bw; cc += blockDim.x) dst[cc] = tile[(size_t)rl * bw + cc];
+        }
+        // -- exchange
+        if (!grid_sync(a.bar)) return;
+        // -- winner over all CTAs (identical in every CTA)
+        {
+            Key wk = KeyNone<F>::v();
+            int64_t wr = INT64_MAX;
+            int wb = -1;
+            for (int g = threadIdx.x; g < G; g += blockDim.x) {
+                int64_t rr = ldcg(a.cand_row + par * G + g);
+                if (rr != INT64_MAX) {
+                    Key kk = ldcg(a.cand_key + par * G + g);
+                    if (better(kk, rr, wk, wr)) { wk = kk; wr = rr; wb = g; }
+                }
+            }
+            for (int o = 16; o; o >>= 1) {
+                Key ok = __shfl_down_sync(0xffffffffu, wk, o);
+                int64_t orow = __shfl_down_sync(0xffffffffu, wr, o);
+                int ob = __shfl_down_sync(0xffffffffu, wb, o);
+                if (better(ok, orow, wk, wr)) { wk = ok; wr = orow; wb = ob; }
+            }
+            if (lane == 0) { s_wkey[warp] = wk; s_wrow[warp] = wr; s_wblk[warp] = wb; }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int w = 1; w < NW; ++w)
+                    if (better(s_wkey[w], s_wrow[w], wk, wr)) { wk = s_wkey[w]; wr = s_wrow[w]; wb = s_wblk[w]; }
+                s_win_row = wr;
+                s_win_blk = wb;
+                s_win_ok = (wr != INT64_MAX) && f.is_pivot(wk);
+            }
+            __syncthreads();
+        }
+        if (!s_win_ok) continue;  // column c has no pivot (uniform decision)
+        const int64_t wrow = s_win_row;
+        {
+            const T* src = a.cand_vals + ((size_t)par * G + s_win_blk) * a.b;
+            for (int cc = threadIdx.x; cc < bw; cc += blockDim.x) prow[cc] = ldcg(src + cc);
+            for (int r = threadIdx.x; r < R; r += blockDim.x) fcol[r] = tile[(size_t)r * bw + c];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_inv = f.inv(prow[c]);
+        __syncthreads();
+        {
+            const T piv = prow[c];
+            const T pinv = s_inv;
+            __syncthreads();
+            for (int cc = threadIdx.x; cc < bw; cc += blockDim.x)
+                prow[cc] = (cc == c) ? pinv : f.scale(prow[cc], piv, pinv);
+        }
+        __syncthreads();
+        // -- eliminate own rows (Gauss-Jordan, above and below), keeping the
+        //    transform in column c
+        for (int r = warp; r < R; r += NW) {
+            T* row = tile + (size_t)r * bw;
+            if (r0 + r == wrow) {
+                for (int cc = lane; cc < bw; cc += 32) row[cc] = prow[cc];
+                if (lane == 0) used[r] = 1;
+            } else {
+                const T fv = fcol[r];
+                if (f.nonzero(fv)) {
+                    for (int cc = lane; cc < bw; cc += 32) {
+                        T x = (cc == c) ? f.zero() : row[cc];
+                        row[cc] = f.sub(x, f.mul(fv, prow[cc]));
+                    }
+                }
+            }
+        }
+        if (threadIdx.x == 0) {
+            s_pcols[k] = c;
+            s_prows[k] = wrow;
+            ispiv[c] = k;
+        }
+        ++k;
+        __syncthreads();
+    }
+
+    // -- write back: pivot columns become unit vectors, the transform goes to E
+    if (k > 0) {
+        for (int r = warp; r < R; r += NW) {
+            const int64_t gr = r0 + r;
+            T* dst = a.A + gr * a.lda + a.j0;
+            const T* row = tile + (size_t)r * bw;
+            for (int cc = lane; cc < bw; cc += 32) {
+                const int t = ispiv[cc];
+                if (t >= 0) dst[cc] = (gr == s_prows[t]) ? f.one() : f.zero();
+                else dst[cc] = row[cc];
+            }
+            if (lane == 0) a.row_used[gr] = used[r];
+        }
+    }
+    if (a.E != nullptr) {
+        for (int r = warp; r < R; r += NW) {
+            const int64_t gr = r0 + r;
+            T* e = a.E + gr * a.ldE;
+            const T* row = tile + (size_t)r * bw;
+            for (int t = lane; t < a.b; t += 32) e[t] = (t < k) ? row[s_pcols[t]] : f.zero();
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int t = 0; t < k; ++t) {
+            a.piv_row[rank0 + t] = (int32_t)s_prows[t];
+            a.piv_col[rank0 + t] = a.j0 + s_pcols[t];
+            a.panel_rows[t] = (int32_t)s_prows[t];
+        }
+        *a.panel_k = k;
+        *a.rank = rank0 + k;
+    }
+}
+
+// ----------------------------------------------------------------------------
+// 2. pivot-row gather for the trailing update
+// ----------------------------------------------------------------------------
+template <class F>
+__global__ void gather_pivot_rows_kernel(F f, typename F::T* A, int64_t lda, int64_t j1, int64_t N,
+                                         const int32_t* panel_rows, const int32_t* panel_k,
+                                         typename F::T* Bm, int64_t ldb) {
+    const int t = blockIdx.y;
+    const int k = *panel_k;
+    if (t >= k) return;
+    const int64_t row = panel_rows[t];
+    typename F::T* src = A + row * lda + j1;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        Bm[t * ldb + c] = GemmOps<F>::prep_b(f, src[c]);
+        src[c] = f.zero();
+    }
+}
+
+// ----------------------------------------------------------------------------
+// 3. SIMT trailing update:  A[:, j1:j1+N] += E[:, :k] * Bm[:k, :]
+// ----------------------------------------------------------------------------
+template <class F, int BK, int LAZY>
+__global__ void __launch_bounds__(256) trailing_simt_kernel(F f, typename F::T* A, int64_t lda,
+                                                            int64_t m, int64_t j1, int64_t N,
+                                                            const typename F::T* E, int64_t ldE,
+                                                            const typename F::T* Bm, int64_t ldb,
+                                                            const int32_t* panel_k) {
+    using T = typename F::T;
+    using Ops = GemmOps<F>;
+    using Acc = typename Ops::Acc;
+    constexpr int BM = 64, BN = 128;
+    __shared__ T Es[BM][BK + 1];
+    __shared__ T Bs[BK][BN];
+    const int k = *panel_k;
+    if (k == 0) return;
+    const int64_t bm0 = (int64_t)blockIdx.y * BM;
+    const int64_t bn0 = (int64_t)blockIdx.x * BN;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    Acc acc[4][8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = Ops::acc_zero(f);
+
+    for (int kk = 0; kk < k; kk += BK) {
+        for (int idx = threadIdx.x; idx < BM * BK; idx += blockDim.x) {
+            const int r = idx / BK, t = idx % BK;
+            const int64_t row = bm0 + r;
+            Es[r][t] = (row < m && kk + t < k) ? E[row * ldE + kk + t] : f.zero();
+        }
+        for (int idx = threadIdx.x; idx < BK * BN; idx += blockDim.x) {
+            const int t = idx / BN, cc = idx % BN;
+            Bs[t][cc] = (kk + t < k && bn0 + cc < N) ? Bm[(int64_t)(kk + t) * ldb + bn0 + cc]
+                                                    : Ops::b_zero(f);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int t0 = 0; t0 < BK; t0 += LAZY) {
+#pragma unroll
+            for (int t = t0; t < t0 + LAZY; ++t) {
+                T av[4], bv[8];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) av[i] = Es[ty * 4 + i][t];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) bv[j] = Bs[t][tx + 16 * j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) acc[i][j] = Ops::mac(f, acc[i][j], av[i], bv[j]);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = Ops::fold(f, acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t row = bm0 + ty * 4 + i;
+        if (row >= m) continue;
+        T* dst = A + row * lda + j1;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int64_t col = bn0 + tx + 16 * j;
+            if (col < N) dst[col] = Ops::finish(f, acc[i][j], dst[col]);
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------
+// 4. final gather into RREF row order
+// ----------------------------------------------------------------------------
+template <class T>
+__global__ void gather_rref_rows_kernel(const T* A, int64_t lda, T* out, int64_t ldo, int64_t m,
+                                        int64_t n, const int32_t* piv_row, const int64_t* rank_p,
+                                        T zero) {
+    const int64_t rank = *rank_p;
+    for (int64_t r = blockIdx.y; r < m; r += gridDim.y) {
+        T* dst = out + r * ldo;
+        if (r < rank) {
+            const T* src = A + (int64_t)piv_row[r] * lda;
+            for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+                 c += (int64_t)gridDim.x * blockDim.x)
+                dst[c] = src[c];
+        } else {
+            for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+                 c += (int64_t)gridDim.x * blockDim.x)
+                dst[c] = zero;
+        }
+    }
+}
+
+__global__ void copy_pivots_kernel(const int64_t* piv_col, const int64_t* rank_p, int64_t cap,
+                                   int64_t* out_piv, int64_t* out_rank) {
+    const int64_t rank = *rank_p;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cap;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (out_piv) out_piv[i] = (i < rank) ? piv_col[i] : -1;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && out_rank) *out_rank = rank;
+}
+
+__global__ void publish_status_kernel(const int* err, int* status) {
+    if (*err != 0) atomicExch(status, *err);
+}
+
+// ----------------------------------------------------------------------------
+// host driver
+// ----------------------------------------------------------------------------
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+template <class F>
+static size_t panel_smem_bytes(int rows_per_cta, int bw) {
+    using T = typename F::T;
+    return (size_t)rows_per_cta * bw * sizeof(T) + (size_t)bw * sizeof(T) +
+           (size_t)rows_per_cta * sizeof(T) + (size_t)bw * sizeof(int) + (size_t)rows_per_cta + 16;
+}
+
+template <class F>
+int plan_rref(int64_t m, int64_t n, RrefPlan* plan) {
+    DeviceInfo di;
+    int rc = device_info(&di);
+    if (rc) return rc;
+    if (!di.coop) { set_error("device does not support cooperative launches"); return LNC_ERR_UNSUPPORTED; }
+    int G = (int)std::min<int64_t>(di.sms, m);
+    int R = (int)((m + G - 1) / G);
+    G = (int)((m + R - 1) / R);
+    const size_t budget = (size_t)di.smem_optin - 8 * 1024;  // static smem headroom
+    int b = 0;
+    for (int cand : {128, 112, 96, 80, 64, 48, 32, 16}) {
+        if (panel_smem_bytes<F>(R, cand) <= budget) { b = cand; break; }
+    }
+    if (b == 0) {
+        set_error("matrix too tall for the panel kernel: %lld rows", (long long)m);
+        return LNC_ERR_UNSUPPORTED;
+    }
+    plan->G = G;
+    plan->rows_per_cta = R;
+    plan->b = b;
+    plan->smem = panel_smem_bytes<F>(R, std::min<int64_t>(b, n));
+    return LNC_OK;
+}
+
+template <class F>
+size_t rref_scratch_bytes(int64_t m, int64_t n, const RrefPlan& pl) {
+    using T = typename F::T;
+    const int64_t kmax = std::min(m, n);
+    size_t s = 0;
+    s += align_up((size_t)m, 256);                              // row_used
+    s += align_up(sizeof(int32_t) * (size_t)std::max<int64_t>(kmax, 1), 256);  // piv_row
+    s += align_up(sizeof(int64_t) * (size_t)std::max<int64_t>(kmax, 1), 256);  // piv_col
+    s += 256;                                                   // scalars
+    s += align_up(sizeof(int32_t) * kMaxPanel, 256);            // panel_rows
+    s += align_up(sizeof(typename F::Key) * 2 * pl.G, 256);     // cand_key
+    s += align_up(sizeof(int64_t) * 2 * pl.G, 256);             // cand_row
+    s += align_up(sizeof(T) * 2 * (size_t)pl.G * pl.b, 256);    // cand_vals
+    s += align_up(sizeof(T) * (size_t)m * pl.b, 256);           // E
+    s += align_up(sizeof(T) * (size_t)pl.b * (size_t)std::max<int64_t>(n, 1), 256);  // Bm
+    s += trailing_extra_scratch<F>(m, n, pl);
+    return s;
+}
+
+template <class F>
+int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, typename F::T* out,
+             int64_t ldo, int64_t* dev_piv, int64_t* dev_rank, cudaStream_t s, int flags,
+             void* scratch, size_t scratch_bytes, const RrefPlan& pl) {
+    using T = typename F::T;
+    const int64_t kmax = std::min(m, n);
+    // carve scratch
+    unsigned char* p = (unsigned char*)scratch;
+    auto take = [&](size_t bytes) { void* r = p; p += align_up(bytes, 256); return r; };
+    uint8_t* row_used = (uint8_t*)take((size_t)m);
+    int32_t* piv_row = (int32_t*)take(sizeof(int32_t) * (size_t)std::max<int64_t>(kmax, 1));
+    int64_t* piv_col = (int64_t*)take(sizeof(int64_t) * (size_t)std::max<int64_t>(kmax, 1));
+    unsigned char* scal = (unsigned char*)take(256);
+    int64_t* rank = (int64_t*)scal;
+    int32_t* panel_k = (int32_t*)(scal + 8);
+    unsigned* bar_count = (unsigned*)(scal + 16);
+    unsigned* bar_gen = (unsigned*)(scal + 20);
+    int* err = (int*)(scal + 24);
+    int32_t* panel_rows = (int32_t*)take(sizeof(int32_t) * kMaxPanel);
+    typename F::Key* cand_key = (typename F::Key*)take(sizeof(typename F::Key) * 2 * pl.G);
+    int64_t* cand_row = (int64_t*)take(sizeof(int64_t) * 2 * pl.G);
+    T* cand_vals = (T*)take(sizeof(T) * 2 * (size_t)pl.G * pl.b);
+    T* E = (T*)take(sizeof(T) * (size_t)m * pl.b);
+    T* Bm = (T*)take(sizeof(T) * (size_t)pl.b * (size_t)std::max<int64_t>(n, 1));
+    void* extra = (void*)p;
+    if ((size_t)(p - (unsigned char*)scratch) > scratch_bytes) {
+        set_error("internal: scratch layout overflow");
+        return LNC_ERR_INVALID;
+    }
+    int* status = rref_status_symbol_address();
+    if (!status) { set_error("cannot resolve the status word"); return LNC_ERR_CUDA; }
+
+    LNC_CUDA(cudaMemsetAsync(row_used, 0, (size_t)m, s));
+    LNC_CUDA(cudaMemsetAsync(scal, 0, 256, s));
+
+    // input preparation
+    {
+        dim3 grid((unsigned)std::min<int64_t>((n + 255) / 256, 64), (unsigned)std::min<int64_t>(m, 65535));
+        if constexpr (F::kDtype == 1 || F::kDtype == 2) {
+            reduce_input_kernel<F><<<grid, 256, 0, s>>>(f, A, lda, m, n);
+            LNC_CHECK_LAUNCH("reduce_input_kernel");
+        } else {
+            if (!(flags & LNC_FLAG_NO_SCALING)) {
+                row_scale_kernel<F><<<(unsigned)std::min<int64_t>(m, 65535), 256, 0, s>>>(f, A, lda, m, n);
+                LNC_CHECK_LAUNCH("row_scale_kernel");
+            }
+        }
+    }
+
+    auto kpanel = panel_kernel<F>;
+    const size_t smem_max = panel_smem_bytes<F>(pl.rows_per_cta, pl.b);
+    LNC_CUDA(cudaFuncSetAttribute(kpanel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+
+    TrailingCtx<F> tctx;
+    tctx.f = f;
+    tctx.m = m;
+    tctx.n = n;
+    tctx.A = A;
+    tctx.lda = lda;
+    tctx.E = E;
+    tctx.ldE = pl.b;
+    tctx.Bm = Bm;
+    tctx.panel_k = panel_k;
+    tctx.extra = extra;
+    tctx.b = pl.b;
+    tctx.force_simt = (flags & LNC_FLAG_SIMT_TRAILING) != 0;
+
+    for (int64_t j0 = 0; j0 < n; j0 += pl.b) {
+        const int bw = (int)std::min<int64_t>(pl.b, n - j0);
+        const int64_t j1 = j0 + bw;
+        const int64_t N = n - j1;
+        PanelArgs<F> pa;
+        pa.f = f;
+        pa.A = A;
+        pa.lda = lda;
+        pa.m = m;
+        pa.j0 = j0;
+        pa.bw = bw;
+        pa.b = pl.b;
+        pa.row_used = row_used;
+        pa.rank = rank;
+        pa.piv_row = piv_row;
+        pa.piv_col = piv_col;
+        pa.panel_k = panel_k;
+        pa.panel_rows = panel_rows;
+        pa.E = (N > 0) ? E : nullptr;
+        pa.ldE = pl.b;
+        pa.cand_key = cand_key;
+        pa.cand_row = cand_row;
+        pa.cand_vals = cand_vals;
+        pa.bar.count = bar_count;
+        pa.bar.gen = bar_gen;
+        pa.bar.err = err;
+        pa.bar.status = status;
+        pa.rows_per_cta = pl.rows_per_cta;
+        {
+            ScopedKernelTimer kt(KC_PANEL, s);
+            void* args[] = {&pa};
+            const size_t smem = panel_smem_bytes<F>(pl.rows_per_cta, bw);
+            LNC_CUDA(cudaLaunchCooperativeKernel((const void*)kpanel, dim3(pl.G), dim3(kPanelThreads), args,
+                                                 smem, s));
+            LNC_CHECK_LAUNCH("panel_kernel");
+        }
+        if (N > 0) {
+            dim3 grid((unsigned)std::min<int64_t>((N + 255) / 256, 1024), (unsigned)pl.b);
+            gather_pivot_rows_kernel<F><<<grid, 256, 0, s>>>(f, A, lda, j1, N, panel_rows, panel_k, Bm, N);
+            LNC_CHECK_LAUNCH("gather_pivot_rows_kernel");
+            tctx.j1 = j1;
+            tctx.N = N;
+            tctx.ldb = N;
+            int rc = trailing_update<F>(tctx, s);
+            if (rc) return rc;
+        }
+    }
+    {
+        ScopedKernelTimer kt(KC_GATHER, s);
+        dim3 grid((unsigned)std::min<int64_t>((n + 255) / 256, 16), (unsigned)std::min<int64_t>(m, 65535));
+        T zero;
+        memset(&zero, 0, sizeof(T));
+        gather_rref_rows_kernel<T><<<grid, 256, 0, s>>>(A, lda, out, ldo, m, n, piv_row, rank, zero);
+        LNC_CHECK_LAUNCH("gather_rref_rows_kernel");
+    }
+    if (dev_piv || dev_rank) {
+        copy_pivots_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((kmax + 255) / 256, 1024)), 256, 0, s>>>(
+            piv_col, rank, kmax, dev_piv, dev_rank);
+        LNC_CHECK_LAUNCH("copy_pivots_kernel");
+    }
+    publish_status_kernel<<<1, 1, 0, s>>>(err, status);
+    LNC_CHECK_LAUNCH("publish_status_kernel");
+    return LNC_OK;
+}
+
+// ----------------------------------------------------------------------------
+// SIMT trailing update dispatch (the tensor-core path lives in trailing_tc.cu)
+// ----------------------------------------------------------------------------
+template <class F>
+int trailing_update_simt(const TrailingCtx<F>& t, cudaStream_t s) {
+    dim3 grid((unsigned)((t.N + 127) / 128), (unsigned)((t.m + 63) / 64));
+    if (grid.y > 65535) { set_error("trailing update: too many row tiles"); return LNC_ERR_UNSUPPORTED; }
+    ScopedKernelTimer kt(KC_TRAILING, s);
+    if constexpr (F::kDtype == 1) {
+        if (t.f.p < (1u << 31))
+            trailing_simt_kernel<F, 32, 4><<<grid, 256, 0, s>>>(t.f, t.A, t.lda, t.m, t.j1, t.N, t.E, t.ldE, t.Bm, t.ldb, t.panel_k);
+        else
+            trailing_simt_kernel<F, 32, 1><<<grid, 256, 0, s>>>(t.f, t.A, t.lda, t.m, t.j1, t.N, t.E, t.ldE, t.Bm, t.ldb, t.panel_k);
+    } else if constexpr (F::kDtype == 4) {
+        trailing_simt_kernel<F, 8, 1><<<grid, 256, 0, s>>>(t.f, t.A, t.lda, t.m, t.j1, t.N, t.E, t.ldE, t.Bm, t.ldb, t.panel_k);
+    } else {
+        trailing_simt_kernel<F, 16, 1><<<grid, 256, 0, s>>>(t.f, t.A, t.lda, t.m, t.j1, t.N, t.E, t.ldE, t.Bm, t.ldb, t.panel_k);
+    }
+    LNC_CHECK_LAUNCH("trailing_simt_kernel");
+    return LNC_OK;
+}
+
+template int trailing_update_simt<FieldU32>(const TrailingCtx<FieldU32>&, cudaStream_t);
+template int trailing_update_simt<FieldU64>(const TrailingCtx<FieldU64>&, cudaStream_t);
+template int trailing_update_simt<FieldF64>(const TrailingCtx<FieldF64>&, cudaStream_t);
+template int trailing_update_simt<FieldC128>(const TrailingCtx<FieldC128>&, cudaStream_t);
+
+// ----------------------------------------------------------------------------
+// public entry (dtype dispatch, scratch allocation)
+// ----------------------------------------------------------------------------
+template <class F>
+static int rref_device_typed(const F& f, void* work, int64_t ldw, void* out, int64_t ldo, int64_t m,
+                             int64_t n, int64_t* dev_piv, int64_t* dev_rank, cudaStream_t s, int flags) {
+    using T = typename F::T;
+    RrefPlan pl;
+    int rc = plan_rref<F>(m, n, &pl);
+    if (rc) return rc;
+    size_t sb = rref_scratch_bytes<F>(m, n, pl);
+    const bool in_place = (out == work);
+    if (in_place) sb += align_up(sizeof(T) * (size_t)m * (size_t)n, 256);
+    void* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, sb, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device scratch allocation of %zu bytes failed: %s", sb, cudaGetErrorString(e));
+        return LNC_ERR_OOM;
+    }
+    T* out_t = (T*)out;
+    int64_t ldo_t = ldo;
+    T* tmp = nullptr;
+    if (in_place) {
+        tmp = (T*)((unsigned char*)scratch + rref_scratch_bytes<F>(m, n, pl));
+        out_t = tmp;
+        ldo_t = n;
+    }
+    rc = rref_run<F>(f, (T*)work, m, n, ldw, out_t, ldo_t, dev_piv, dev_rank, s, flags, scratch,
+                     rref_scratch_bytes<F>(m, n, pl), pl);
+    if (rc == LNC_OK && in_place) {
+        e = cudaMemcpy2DAsync(out, sizeof(T) * ldo, tmp, sizeof(T) * n, sizeof(T) * n, m,
+                              cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) rc = cuda_status(e, "cudaMemcpy2DAsync");
+    }
+    cudaFreeAsync(scratch, s);
+    return rc;
+}
+
+int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* work,
+                         int64_t ldw, void* out, int64_t ldo, int64_t* dev_piv, int64_t* dev_rank,
+                         cudaStream_t s, int flags) {
+    switch (dtype) {
+        case LNC_U32: return rref_device_typed(FieldU32::make(p), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        case LNC_U64: return rref_device_typed(FieldU64::make(p), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        case LNC_F64: return rref_device_typed(FieldF64::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        case LNC_C128: return rref_device_typed(FieldC128::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        default: set_error("unknown dtype %d", dtype); return LNC_ERR_INVALID;
+    }
+}
+
+}  // namespace lnc

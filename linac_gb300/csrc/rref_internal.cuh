@@ -1,0 +1,164 @@
+// Internal declarations shared by rref.cu and trailing_tc.cu.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "field.cuh"
+#include "sync.cuh"
+
+namespace lnc {
+
+struct RrefPlan {
+    int G = 0;             // CTAs of the cooperative panel kernel
+    int rows_per_cta = 0;  // panel rows held by each CTA
+    int b = 0;             // panel width (columns)
+    size_t smem = 0;
+};
+
+template <class F>
+struct PanelArgs {
+    F f;
+    typename F::T* A;
+    int64_t lda;
+    int64_t m;
+    int64_t j0;
+    int bw;                 // width of this panel
+    int b;                  // nominal panel width (E / exchange leading dims)
+    uint8_t* row_used;      // 1 once a row is a pivot row
+    int64_t* rank;          // pivots found before this panel (updated)
+    int32_t* piv_row;       // physical row of pivot t
+    int64_t* piv_col;       // column of pivot t
+    int32_t* panel_k;       // pivots found in this panel
+    int32_t* panel_rows;    // their physical rows
+    typename F::T* E;       // m x ldE transform columns (may be null)
+    int64_t ldE;
+    typename F::Key* cand_key;  // [2][G] per-CTA proposals
+    int64_t* cand_row;          // [2][G]
+    typename F::T* cand_vals;   // [2][G][b] proposed rows
+    GridBarrier bar;
+    int rows_per_cta;
+};
+
+// Multiply-accumulate policy of the SIMT trailing update, per field.
+template <class F> struct GemmOps;
+
+template <> struct GemmOps<FieldU32> {
+    using Acc = uint64_t;
+    static __device__ __forceinline__ Acc acc_zero(const FieldU32&) { return 0ull; }
+    static __device__ __forceinline__ uint32_t b_zero(const FieldU32&) { return 0u; }
+    static __device__ __forceinline__ uint32_t prep_b(const FieldU32&, uint32_t v) { return v; }
+    // lazy accumulation: the caller folds after LAZY products (LAZY = 4 for
+    // p < 2^31 keeps acc < p + 4 (p-1)^2 < 2^64)
+    static __device__ __forceinline__ Acc mac(const FieldU32&, Acc acc, uint32_t a, uint32_t b) {
+        return acc + (uint64_t)a * b;
+    }
+    static __device__ __forceinline__ Acc fold(const FieldU32& f, Acc acc) { return f.reduce64(acc); }
+    static __device__ __forceinline__ uint32_t finish(const FieldU32& f, Acc acc, uint32_t c) {
+        return f.add(c, f.reduce64(acc));
+    }
+};
+
+template <> struct GemmOps<FieldU64> {
+    using Acc = uint64_t;
+    static __device__ __forceinline__ Acc acc_zero(const FieldU64&) { return 0ull; }
+    static __device__ __forceinline__ uint64_t b_zero(const FieldU64&) { return 0ull; }
+    // the B operand is kept in Montgomery form so that one REDC per product
+    // yields the ordinary residue
+    static __device__ __forceinline__ uint64_t prep_b(const FieldU64& f, uint64_t v) { return f.to_mont(v); }
+    static __device__ __forceinline__ Acc mac(const FieldU64& f, Acc acc, uint64_t a, uint64_t b) {
+        return f.add(acc, f.montmul(a, b));
+    }
+    static __device__ __forceinline__ Acc fold(const FieldU64&, Acc acc) { return acc; }
+    static __device__ __forceinline__ uint64_t finish(const FieldU64& f, Acc acc, uint64_t c) {
+        return f.add(c, acc);
+    }
+};
+
+template <> struct GemmOps<FieldF64> {
+    using Acc = double;
+    static __device__ __forceinline__ Acc acc_zero(const FieldF64&) { return 0.0; }
+    static __device__ __forceinline__ double b_zero(const FieldF64&) { return 0.0; }
+    static __device__ __forceinline__ double prep_b(const FieldF64&, double v) { return v; }
+    static __device__ __forceinline__ Acc mac(const FieldF64&, Acc acc, double a, double b) {
+        return fma(a, b, acc);
+    }
+    static __device__ __forceinline__ Acc fold(const FieldF64&, Acc acc) { return acc; }
+    static __device__ __forceinline__ double finish(const FieldF64&, Acc acc, double c) { return c + acc; }
+};
+
+template <> struct GemmOps<FieldC128> {
+    using Acc = c128;
+    static __device__ __forceinline__ Acc acc_zero(const FieldC128& f) { return f.zero(); }
+    static __device__ __forceinline__ c128 b_zero(const FieldC128& f) { return f.zero(); }
+    static __device__ __forceinline__ c128 prep_b(const FieldC128&, c128 v) { return v; }
+    static __device__ __forceinline__ Acc mac(const FieldC128&, Acc acc, c128 a, c128 b) {
+        acc.x = fma(a.x, b.x, acc.x);
+        acc.x = fma(-a.y, b.y, acc.x);
+        acc.y = fma(a.x, b.y, acc.y);
+        acc.y = fma(a.y, b.x, acc.y);
+        return acc;
+    }
+    static __device__ __forceinline__ Acc fold(const FieldC128&, Acc acc) { return acc; }
+    static __device__ __forceinline__ c128 finish(const FieldC128&, Acc acc, c128 c) {
+        c.x += acc.x;
+        c.y += acc.y;
+        return c;
+    }
+};
+
+__device__ __forceinline__ double scale_real(double x, double s) { return x / s; }
+__device__ __forceinline__ c128 scale_real(c128 x, double s) {
+    c128 r;
+    r.x = x.x / s;
+    r.y = x.y / s;
+    return r;
+}
+
+// Everything a trailing-update implementation needs for one panel.
+template <class F>
+struct TrailingCtx {
+    F f;
+    int64_t m = 0, n = 0;
+    typename F::T* A = nullptr;
+    int64_t lda = 0;
+    const typename F::T* E = nullptr;  // m x ldE, transform columns
+    int64_t ldE = 0;
+    const typename F::T* Bm = nullptr; // k x ldb, pivot rows' trailing part
+    int64_t ldb = 0;
+    const int32_t* panel_k = nullptr;
+    void* extra = nullptr;             // scratch reserved by trailing_extra_scratch
+    int b = 0;
+    int64_t j1 = 0, N = 0;             // trailing columns [j1, j1 + N)
+    bool force_simt = false;
+};
+
+template <class F>
+int trailing_update_simt(const TrailingCtx<F>& t, cudaStream_t s);
+
+// Tensor-core trailing update for 32-bit residues (trailing_tc.cu).
+int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s);
+size_t trailing_tc_u32_scratch(int64_t m, int64_t n, int b);
+bool trailing_tc_u32_available();
+
+template <class F>
+inline size_t trailing_extra_scratch(int64_t m, int64_t n, const RrefPlan& pl) {
+    if constexpr (F::kDtype == 1) return trailing_tc_u32_scratch(m, n, pl.b);
+    return 0;
+}
+
+template <class F>
+inline int trailing_update(const TrailingCtx<F>& t, cudaStream_t s) {
+    if constexpr (F::kDtype == 1) {
+        if (!t.force_simt && trailing_tc_u32_available()) return trailing_update_tc_u32(t, s);
+    }
+    return trailing_update_simt<F>(t, s);
+}
+
+int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* work,
+                         int64_t ldw, void* out, int64_t ldo, int64_t* dev_piv, int64_t* dev_rank,
+                         cudaStream_t s, int flags);
+int rref_read_and_clear_status(int* status);
+
+}  // namespace lnc

@@ -1,0 +1,75 @@
+// Bounded device-side synchronisation helpers.
+//
+// Every spin-wait in this library has a time limit: when it runs out the
+// waiting CTA records LNC_ERR_TIMEOUT in the call's error word and in the
+// module's status word, stops waiting and returns, so that the host sees an
+// error status instead of a hung GPU.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lnc {
+
+// ~2 s at the GB300 maximum SM clock (2.07 GHz); an ordinary barrier wait is
+// a few microseconds.
+constexpr long long kSpinLimitCycles = 4000000000ll;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int ld_volatile_i32(const int* p) {
+    return *(const volatile int*)p;
+}
+
+struct GridBarrier {
+    unsigned* count;   // arrivals in the current generation
+    unsigned* gen;     // generation counter
+    int* err;          // call-wide error word (0 = ok)
+    int* status;       // module status word read by lnc_device_status()
+};
+
+// Grid-wide barrier for a cooperative launch (all CTAs co-resident).  Returns
+// false (uniformly within the CTA) when the wait timed out or another CTA
+// reported an error; the caller must then return.
+__device__ __forceinline__ bool grid_sync(const GridBarrier& b) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
+        unsigned g = ld_acquire_u32(b.gen);
+        __threadfence();
+        unsigned arrived = atomicAdd(b.count, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(b.count, 0u);
+            __threadfence();
+            st_release_u32(b.gen, g + 1);
+        } else {
+            long long t0 = clock64();
+            while (ld_acquire_u32(b.gen) == g) {
+                if (ld_volatile_i32(b.err) != 0) { ok = 0; break; }
+                if (clock64() - t0 > kSpinLimitCycles) {
+                    atomicExch(b.err, -5);
+                    atomicExch(b.status, -5);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_ok = ok && (ld_volatile_i32(b.err) == 0);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+}  // namespace lnc

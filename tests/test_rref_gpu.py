@@ -92,7 +92,8 @@ def test_rank_deficient_vs_oracle(m, n, r, p):
         A = workloads.rank_deficient_modp(m, n, r, p, rng)
     R, piv = cuda_row_reduce(A, p, return_pivots=True)
     R_ref, piv_ref, rank_ref = oracle.rref_modp(A, p)
-    assert rank_ref == min(r, m, n)
+    if p > 2**16:  # over a small field B.C loses rank with noticeable probability
+        assert rank_ref == min(r, m, n)
     assert np.array_equal(R.astype(np.uint64), R_ref)
     assert piv == piv_ref
 

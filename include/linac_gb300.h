@@ -118,6 +118,23 @@ int lnc_rref_device(int dtype, int64_t m, int64_t n, uint64_t p, double tol, voi
                     int64_t ld_work, void* dev_out, int64_t ld_out, int64_t* dev_pivot_cols,
                     int64_t* dev_rank, void* stream, int flags);
 
+/*
+ * The same device RREF as lnc_rref_device, but allocating nothing: its scratch
+ * is a fixed 16 MiB array in the library's device memory instead of
+ * stream-ordered allocations.  For callers that cannot allocate device memory
+ * when they need the result -- a host framework that reserved all of HBM for
+ * its own pool up front, or a latency-critical thread that must not wait on an
+ * allocator.  No counterpart in the reference (linac always allocates through
+ * pycuda).  Limits: dev_out must differ from dev_work; sizes whose scratch
+ * exceeds 16 MiB (about m + n > 30,000 for uint32 residues) are rejected with
+ * LNC_ERR_INVALID.  The first call on a device looks up the array's device
+ * address (make it before any stream capture); all calls share the array, so
+ * calls that overlap on the GPU race.
+ */
+int lnc_rref_device_noalloc(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* dev_work,
+                            int64_t ld_work, void* dev_out, int64_t ld_out, int64_t* dev_pivot_cols,
+                            int64_t* dev_rank, void* stream, int flags);
+
 /* ---- monomial loader --------------------------------------------------------- */
 /*
  * out[r, c] = prod_{t<degree} bases[r, lindices[c, t]] (mod p for LNC_U32 /

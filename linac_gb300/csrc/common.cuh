@@ -62,6 +62,7 @@ int device_info(DeviceInfo* out);
 
 size_t dtype_size(int dtype);
 bool is_prime_u64(uint64_t n);
+int validate_rref_args(int dtype, int64_t m, int64_t n, uint64_t p, int64_t ld);
 
 constexpr int kMaxPanel = 128;           // widest panel (columns)
 constexpr int kPanelThreads = 256;

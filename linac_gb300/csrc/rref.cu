@@ -695,4 +695,95 @@ int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol
     }
 }
 
+// ----------------------------------------------------------------------------
+// No-allocation variant: the same RREF with its scratch in a fixed, file-scope
+// device array instead of stream-ordered allocations.
+//
+// Some callers cannot allocate device memory at the time they need an RREF:
+// a host framework that has reserved all of HBM for its own pool allocator
+// up front (so cudaMalloc / cudaMallocAsync fail or steal from it), or a
+// latency-critical serving thread that must never wait on an allocator.  For
+// them the scratch lives in g_noalloc_scratch, a 16 MiB array that every GPU
+// loading this library holds until the process exits.  Requests whose
+// scratch does not fit are rejected up front with LNC_ERR_INVALID.
+//
+// The array's name in host code is only a host-side stand-in; the device
+// address is obtained once per device with cudaGetSymbolAddress, on that
+// device's first call of lnc_rref_device_noalloc (so make that first call
+// before any stream capture).  All calls share the array and it keeps the
+// previous call's contents; the driver clears everything that must start at
+// zero.  Calls that overlap on the GPU (concurrent streams, or devices not
+// yet synchronised between calls) race on the array.
+// ----------------------------------------------------------------------------
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[64] = {};
+
+static int noalloc_scratch(void** out) {
+    int dev = 0;
+    LNC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) { set_error("device index out of range"); return LNC_ERR_INVALID; }
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(no-allocation scratch)");
+        g_noalloc_ptr[dev] = ptr;
+    }
+    *out = g_noalloc_ptr[dev];
+    return LNC_OK;
+}
+
+template <class F>
+static int rref_noalloc_typed(const F& f, void* work, int64_t ldw, void* out, int64_t ldo, int64_t m, int64_t n,
+                              int64_t* dev_piv, int64_t* dev_rank, cudaStream_t s, int flags) {
+    using T = typename F::T;
+    RrefPlan pl;
+    int rc = plan_rref<F>(m, n, &pl);
+    if (rc) return rc;
+    const size_t need = rref_scratch_bytes<F>(m, n, pl);
+    if (need > kNoAllocScratchBytes) {
+        set_error("a %lld x %lld RREF needs %zu bytes of scratch; the fixed no-allocation scratch holds %zu",
+                  (long long)m, (long long)n, need, kNoAllocScratchBytes);
+        return LNC_ERR_INVALID;
+    }
+    void* scratch = nullptr;
+    rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    return rref_run<F>(f, (T*)work, m, n, ldw, (T*)out, ldo, dev_piv, dev_rank, s, flags, scratch, need, pl);
+}
+
+int rref_device_noalloc_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* work,
+                                 int64_t ldw, void* out, int64_t ldo, int64_t* dev_piv, int64_t* dev_rank,
+                                 cudaStream_t s, int flags) {
+    if (out == work) {
+        set_error("the no-allocation RREF needs distinct input and output buffers");
+        return LNC_ERR_INVALID;
+    }
+    switch (dtype) {
+        case LNC_U32: return rref_noalloc_typed(FieldU32::make(p), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        case LNC_U64: return rref_noalloc_typed(FieldU64::make(p), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        case LNC_F64: return rref_noalloc_typed(FieldF64::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        case LNC_C128: return rref_noalloc_typed(FieldC128::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        default: set_error("unknown dtype %d", dtype); return LNC_ERR_INVALID;
+    }
+}
+
 }  // namespace lnc
+
+extern "C" int lnc_rref_device_noalloc(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* dev_work,
+                                       int64_t ld_work, void* dev_out, int64_t ld_out, int64_t* dev_pivot_cols,
+                                       int64_t* dev_rank, void* stream, int flags) {
+    using namespace lnc;
+    int rc = validate_rref_args(dtype, m, n, p, ld_work);
+    if (rc) return rc;
+    if (ld_out < n) { set_error("output leading dimension %lld < n", (long long)ld_out); return LNC_ERR_INVALID; }
+    if (m == 0 || n == 0) {
+        set_error("the no-allocation RREF needs a non-empty matrix");
+        return LNC_ERR_INVALID;
+    }
+    return rref_device_noalloc_dispatch(dtype, m, n, p, tol, dev_work, ld_work, dev_out, ld_out, dev_pivot_cols,
+                                        dev_rank, (cudaStream_t)stream, flags);
+}

@@ -548,6 +548,9 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
     tctx.ldE = pl.b;
     tctx.Bm = Bm;
     tctx.panel_k = panel_k;
+    tctx.panel_rows = panel_rows;
+    tctx.err = err;
+    tctx.status = status;
     tctx.extra = extra;
     tctx.b = pl.b;
     tctx.force_simt = (flags & LNC_FLAG_SIMT_TRAILING) != 0;
@@ -589,9 +592,6 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
             LNC_CHECK_LAUNCH("panel_kernel");
         }
         if (N > 0) {
-            dim3 grid((unsigned)std::min<int64_t>((N + 255) / 256, 1024), (unsigned)pl.b);
-            gather_pivot_rows_kernel<F><<<grid, 256, 0, s>>>(f, A, lda, j1, N, panel_rows, panel_k, Bm, N);
-            LNC_CHECK_LAUNCH("gather_pivot_rows_kernel");
             tctx.j1 = j1;
             tctx.N = N;
             tctx.ldb = N;
@@ -622,6 +622,12 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
 // ----------------------------------------------------------------------------
 template <class F>
 int trailing_update_simt(const TrailingCtx<F>& t, cudaStream_t s) {
+    {
+        dim3 g((unsigned)std::min<int64_t>((t.N + 255) / 256, 1024), (unsigned)t.b);
+        gather_pivot_rows_kernel<F><<<g, 256, 0, s>>>(t.f, t.A, t.lda, t.j1, t.N, t.panel_rows, t.panel_k,
+                                                     const_cast<typename F::T*>(t.Bm), t.ldb);
+        LNC_CHECK_LAUNCH("gather_pivot_rows_kernel");
+    }
     dim3 grid((unsigned)((t.N + 127) / 128), (unsigned)((t.m + 63) / 64));
     if (grid.y > 65535) { set_error("trailing update: too many row tiles"); return LNC_ERR_UNSUPPORTED; }
     ScopedKernelTimer kt(KC_TRAILING, s);

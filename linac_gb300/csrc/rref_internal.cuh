@@ -128,6 +128,9 @@ struct TrailingCtx {
     const typename F::T* Bm = nullptr; // k x ldb, pivot rows' trailing part
     int64_t ldb = 0;
     const int32_t* panel_k = nullptr;
+    const int32_t* panel_rows = nullptr;  // physical rows of this panel's pivots
+    int* err = nullptr;                // call-wide error word
+    int* status = nullptr;             // module status word
     void* extra = nullptr;             // scratch reserved by trailing_extra_scratch
     int b = 0;
     int64_t j1 = 0, N = 0;             // trailing columns [j1, j1 + N)

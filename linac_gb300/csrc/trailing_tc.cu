@@ -1,14 +1,452 @@
-// Tensor-core trailing update for 32-bit residues (placeholder until the
-// tcgen05 limb kernel lands): reports itself unavailable so the driver uses
-// the SIMT contraction.
+// Exact F_p trailing update on the tcgen05 tensor cores (32-bit residues).
+//
+//   C[:, T] <- C[:, T] + E * B   (mod p),  E: m x K transform, B: K x N pivot rows
+//
+// The reference has no counterpart for this step: linac eliminates one column
+// at a time with a 64-bit `%` per element (linac/row_reduce.cu:107-114,
+// 138-196).  Here the whole panel (K = 128 pivots) is applied in one
+// contraction, exactly, on the BF16 tensor cores:
+//
+//  * every residue x (centred to (-p/2, p/2)) is split into four balanced
+//    base-256 digits x = sum_i d_i 256^i, d_i in [-128, 128]; integers of that
+//    size are exact in BF16;
+//  * a digit product is at most 2^14 in magnitude, and the four products that
+//    share a weight 256^s (s = i + j) summed over K = 128 stay below 2^23, so
+//    every FP32 accumulation in TMEM is an exact integer;
+//  * the epilogue converts the seven group sums D_s to integers, forms
+//    sum_s D_s * (256^s mod p) in 64-bit, reduces it mod p (Barrett) and adds
+//    it to the old residue.
+//
+// Layout: the four E digit planes are K-major (row = matrix row, 128 digits),
+// the B digits are stacked per 64-column output tile as 4 x 64 K-major rows, so
+// one UMMA (M = 128, N = 256, K = 16) multiplies digit plane i of E with all
+// four digit planes of B and lands in TMEM columns [64 i, 64 i + 256): the
+// column block s = i + j accumulates exactly the weight-256^s products.
+//
+// Kernel: one CTA per 128-row block and up to 8 consecutive 64-column tiles;
+// warp 0 issues TMA loads (E digits once, B digits double-buffered), warp 1
+// issues the UMMAs and owns the TMEM allocation, warps 2-5 drain TMEM, combine,
+// write C and re-zero their TMEM lanes for the next tile.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
 #include "rref_internal.cuh"
+#include "tc_ptx.cuh"
 
 namespace lnc {
+namespace tc {
 
-bool trailing_tc_u32_available() { return false; }
-size_t trailing_tc_u32_scratch(int64_t, int64_t, int) { return 0; }
+constexpr int BM = 128;                 // tile rows (TMEM lanes)
+constexpr int BN = 64;                  // output columns per tile
+constexpr int LIMBS = 4;                // base-256 digits per residue
+constexpr int KMAX = 128;               // contraction depth (panel width)
+constexpr int KC = 64;                  // K per stage: one 128-byte swizzle row of BF16
+constexpr int NKC = KMAX / KC;          // 2
+constexpr int GROUPS = 2 * LIMBS - 1;   // 7 weights 256^0 .. 256^6
+constexpr int B_ROWS = LIMBS * BN;      // 256 stacked digit rows per output tile
+constexpr int STAGES = 2;
+constexpr int TILES_PER_CTA = 8;
+constexpr int THREADS = 192;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t A_TILE_BYTES = BM * KC * 2;      // 16 KB
+constexpr uint32_t B_TILE_BYTES = B_ROWS * KC * 2;  // 32 KB
+constexpr uint32_t A_BYTES = LIMBS * NKC * A_TILE_BYTES;  // 128 KB
+constexpr uint32_t SMEM_BYTES = A_BYTES + STAGES * B_TILE_BYTES + 1024 /*barriers*/ + 1024 /*align*/;
+
+struct TcParams {
+    uint32_t* C;            // trailing block base: A + j1
+    int64_t ldc;
+    int64_t m;
+    int64_t N;
+    int m_pad;              // rows per digit plane in the E operand
+    int n_tiles;            // 64-column tiles covering N
+    const int32_t* panel_k;
+    FieldU32 f;
+    int32_t w[GROUPS];      // 256^s mod p, centred
+    uint64_t off;           // multiple of p >= 2^59 (makes the 64-bit sum non-negative)
+    int* err;
+    int* status;
+};
+
+__device__ __forceinline__ void split_digits(uint32_t x, uint32_t p, uint32_t half, __nv_bfloat16 (&d)[LIMBS]) {
+    int32_t v = (x > half) ? (int32_t)((int64_t)x - (int64_t)p) : (int32_t)x;
+#pragma unroll
+    for (int i = 0; i < LIMBS - 1; ++i) {
+        const int32_t di = ((v + 128) & 255) - 128;
+        d[i] = __float2bfloat16_rn((float)di);
+        v = (v - di) >> 8;
+    }
+    d[LIMBS - 1] = __float2bfloat16_rn((float)v);  // |v| <= 128
+}
+
+// E (m x ldE residues, columns >= k are zero) -> four K-major digit planes of
+// m_pad x 128 BF16.
+__global__ void split_e_kernel(const uint32_t* E, int64_t ldE, int b, int64_t m, int m_pad, uint32_t p,
+                               const int32_t* panel_k, __nv_bfloat16* EL) {
+    const int k = *panel_k;
+    if (k == 0) return;
+    const uint32_t half = p >> 1;
+    const size_t plane = (size_t)m_pad * KMAX;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)m_pad * KMAX;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / KMAX;
+        const int t = (int)(idx - r * KMAX);
+        uint32_t x = (r < m && t < k && t < b) ? E[r * ldE + t] : 0u;
+        __nv_bfloat16 d[LIMBS];
+        split_digits(x, p, half, d);
+#pragma unroll
+        for (int i = 0; i < LIMBS; ++i) EL[i * plane + idx] = d[i];
+    }
+}
+
+// Pivot rows of the trailing block -> stacked digit rows (one CTA per 64-column
+// tile), zeroing those rows in C.
+__global__ void __launch_bounds__(256) gather_split_b_kernel(uint32_t* C, int64_t ldc, int64_t N,
+                                                             const int32_t* panel_rows, const int32_t* panel_k,
+                                                             uint32_t p, __nv_bfloat16* BS) {
+    __shared__ uint32_t s[KMAX][BN + 1];
+    const int k = *panel_k;
+    if (k == 0) return;
+    const int tile = blockIdx.x;
+    const int64_t c0 = (int64_t)tile * BN;
+    const uint32_t half = p >> 1;
+    for (int idx = threadIdx.x; idx < KMAX * BN; idx += blockDim.x) {
+        const int t = idx / BN, cc = idx % BN;
+        uint32_t v = 0;
+        if (t < k && c0 + cc < N) {
+            uint32_t* src = C + (int64_t)panel_rows[t] * ldc + c0 + cc;
+            v = *src;
+            *src = 0u;
+        }
+        s[t][cc] = v;
+    }
+    __syncthreads();
+    // row (i, cc) of this tile's stacked block holds digit i of column cc for t = 0..127
+    __nv_bfloat16* dst = BS + (size_t)tile * B_ROWS * KMAX;
+    for (int idx = threadIdx.x; idx < BN * KMAX; idx += blockDim.x) {
+        const int cc = idx / KMAX, t = idx % KMAX;
+        __nv_bfloat16 d[LIMBS];
+        split_digits(s[t][cc], p, half, d);
+#pragma unroll
+        for (int i = 0; i < LIMBS; ++i) dst[((size_t)i * BN + cc) * KMAX + t] = d[i];
+    }
+}
+
+__device__ __forceinline__ void flag_error(const TcParams& P, volatile int* cta_err) {
+    *cta_err = 1;
+    atomicExch(P.err, LNC_ERR_TIMEOUT);
+    atomicExch(P.status, LNC_ERR_TIMEOUT);
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    limb_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     const TcParams P) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte alignment for the 128-byte swizzle atoms
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* sA = smem;                         // [LIMBS][NKC][BM x KC]
+    unsigned char* sB = smem + A_BYTES;               // [STAGES][B_ROWS x KC]
+    uint64_t* bars = (uint64_t*)(sB + STAGES * B_TILE_BYTES);
+    uint64_t* a_full = bars + 0;
+    uint64_t* b_full = bars + 1;   // [STAGES]
+    uint64_t* b_empty = bars + 3;  // [STAGES]
+    uint64_t* acc_full = bars + 5;
+    uint64_t* acc_empty = bars + 6;
+    uint64_t* drain = bars + 7;
+    uint32_t* s_tmem = (uint32_t*)(bars + 8);
+    __shared__ volatile int s_err;
+
+    const int k = *P.panel_k;  // written by an earlier kernel: identical in every thread
+    if (k == 0) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rb = blockIdx.y;
+    const int t0 = blockIdx.x * TILES_PER_CTA;
+    const int t1 = min(P.n_tiles, t0 + TILES_PER_CTA);
+    const int ntiles = t1 - t0;
+    const int nkc = (k > KC) ? 2 : 1;  // skip the second K chunk when it is all zero
+
+    if (threadIdx.x == 0) {
+        s_err = (ld_volatile_i32(P.err) != 0) ? 1 : 0;  // an earlier kernel of this call failed
+        ptx::mbar_init(a_full, 1);
+        for (int s = 0; s < STAGES; ++s) {
+            ptx::mbar_init(&b_full[s], 1);
+            ptx::mbar_init(&b_empty[s], 1);
+        }
+        ptx::mbar_init(acc_full, 1);
+        ptx::mbar_init(acc_empty, 4);
+        ptx::mbar_init(drain, 1);
+        ptx::fence_mbar_init();
+    }
+    if (warp == 1) {
+        ptx::tmem_alloc(s_tmem, TMEM_COLS);
+        ptx::tmem_relinquish();
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem = *s_tmem;
+
+    if (warp == 0) {
+        // ------------------------------------------------------------ producer
+        if (lane == 0) {
+            ptx::prefetch_tmap(&tmA);
+            ptx::prefetch_tmap(&tmB);
+            ptx::mbar_expect_tx(a_full, LIMBS * nkc * A_TILE_BYTES);
+            for (int i = 0; i < LIMBS; ++i)
+                for (int kc = 0; kc < nkc; ++kc)
+                    ptx::tma_load_2d(sA + (i * NKC + kc) * A_TILE_BYTES, &tmA, a_full, kc * KC,
+                                     i * P.m_pad + rb * BM);
+            int it = 0;
+            int issued_round[STAGES] = {-1, -1};
+            for (int t = 0; t < ntiles && !s_err; ++t) {
+                for (int kc = 0; kc < nkc; ++kc, ++it) {
+                    const int st = it % STAGES, round = it / STAGES;
+                    if (!ptx::mbar_wait(&b_empty[st], (round & 1) ^ 1, &s_err)) { flag_error(P, &s_err); break; }
+                    ptx::mbar_expect_tx(&b_full[st], B_TILE_BYTES);
+                    ptx::tma_load_2d(sB + st * B_TILE_BYTES, &tmB, &b_full[st], kc * KC, (t0 + t) * B_ROWS);
+                    issued_round[st] = round;
+                }
+            }
+            // never leave with copies in flight: wait (bounded) for every load issued
+            const long long lim = kSpinLimitCycles / 4;
+            ptx::mbar_wait_nocancel(a_full, 0, lim);
+            for (int st = 0; st < STAGES; ++st)
+                if (issued_round[st] >= 0) ptx::mbar_wait_nocancel(&b_full[st], issued_round[st] & 1, lim);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = ptx::umma_idesc_bf16(BM, B_ROWS);
+            const uint32_t a_base = ptx::smem_u32(sA);
+            const uint32_t b_base = ptx::smem_u32(sB);
+            bool ok = ptx::mbar_wait(a_full, 0, &s_err);
+            if (!ok) flag_error(P, &s_err);
+            int it = 0;
+            for (int t = 0; t < ntiles && ok; ++t) {
+                if (!ptx::mbar_wait(acc_empty, t & 1, &s_err)) { flag_error(P, &s_err); break; }
+                ptx::tc_fence_after();
+                for (int kc = 0; kc < nkc && ok; ++kc, ++it) {
+                    const int st = it % STAGES, round = it / STAGES;
+                    if (!ptx::mbar_wait(&b_full[st], round & 1, &s_err)) { flag_error(P, &s_err); ok = false; break; }
+                    ptx::tc_fence_after();
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16; ++ks) {
+                        const uint64_t bdesc = ptx::umma_desc_sw128(b_base + st * B_TILE_BYTES + ks * 32);
+#pragma unroll
+                        for (int i = 0; i < LIMBS; ++i) {
+                            const uint64_t adesc =
+                                ptx::umma_desc_sw128(a_base + (i * NKC + kc) * A_TILE_BYTES + ks * 32);
+                            ptx::umma_bf16(tmem + 64u * i, adesc, bdesc, idesc, 1u);
+                        }
+                    }
+                    ptx::umma_commit(&b_empty[st]);  // stage reusable once these UMMAs finish
+                }
+                if (ok) ptx::umma_commit(acc_full);
+            }
+            // all issued UMMAs complete before the TMEM is released
+            ptx::umma_commit(drain);
+            ptx::mbar_wait_nocancel(drain, 0, kSpinLimitCycles / 4);
+        }
+    } else {
+        // ------------------------------------------------------------ epilogue
+        const int q = warp & 3;  // TMEM lane quarter this warp may access
+        const int64_t row = (int64_t)rb * BM + q * 32 + lane;
+        const uint32_t t_lane = tmem + ((uint32_t)(q * 32) << 16);
+        // zero the accumulator (this warp's 32 lanes, 7 x 64 columns)
+        for (int c = 0; c < GROUPS * BN; c += 16) ptx::tmem_st16_zero(t_lane + c);
+        ptx::tmem_st_wait();
+        ptx::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(acc_empty);
+        const FieldU32 f = P.f;
+        for (int t = 0; t < ntiles; ++t) {
+            const int64_t col0 = (int64_t)(t0 + t) * BN;
+            const bool row_ok = row < P.m;
+            uint32_t* crow = P.C + (row_ok ? row : 0) * P.ldc + col0;
+            const int ncols = (int)((P.N - col0) < BN ? (P.N - col0) : BN);
+            uint32_t old[BN];
+            if (row_ok && ncols == BN && ((((uintptr_t)crow) & 15) == 0)) {
+#pragma unroll
+                for (int c = 0; c < BN; c += 4) {
+                    uint4 v = *(const uint4*)(crow + c);
+                    old[c] = v.x; old[c + 1] = v.y; old[c + 2] = v.z; old[c + 3] = v.w;
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < BN; ++c) old[c] = (row_ok && c < ncols) ? crow[c] : 0u;
+            }
+            const bool got = ptx::mbar_wait(acc_full, t & 1, &s_err);
+            if (!__all_sync(0xffffffffu, got)) {  // warp-uniform before the aligned TMEM loads
+                if (lane == 0) flag_error(P, &s_err);
+                break;
+            }
+            ptx::tc_fence_after();
+            const bool vec = row_ok && ncols == BN && ((((uintptr_t)crow) & 15) == 0);
+#pragma unroll
+            for (int cb = 0; cb < BN / 16; ++cb) {
+                uint32_t d[GROUPS][16];
+#pragma unroll
+                for (int s = 0; s < GROUPS; ++s) ptx::tmem_ld16(t_lane + s * BN + cb * 16, d[s]);
+                ptx::tmem_ld_wait();
+                uint32_t res[16];
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    int64_t v = 0;
+#pragma unroll
+                    for (int s = 0; s < GROUPS; ++s)
+                        v += (int64_t)__float2int_rn(__uint_as_float(d[s][c])) * (int64_t)P.w[s];
+                    const uint32_t r = f.reduce64((uint64_t)(v + (int64_t)P.off));
+                    res[c] = f.add(old[cb * 16 + c], r);
+                }
+                if (vec) {
+#pragma unroll
+                    for (int c = 0; c < 16; c += 4)
+                        *(uint4*)(crow + cb * 16 + c) = make_uint4(res[c], res[c + 1], res[c + 2], res[c + 3]);
+                } else if (row_ok) {
+#pragma unroll
+                    for (int c = 0; c < 16; ++c)
+                        if (cb * 16 + c < ncols) crow[cb * 16 + c] = res[c];
+                }
+            }
+            // accumulator drained: re-zero it and hand it back to the MMA warp
+            for (int c = 0; c < GROUPS * BN; c += 16) ptx::tmem_st16_zero(t_lane + c);
+            ptx::tmem_st_wait();
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(acc_empty);
+        }
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    if (warp == 1) ptx::tmem_dealloc(tmem, TMEM_COLS);
+}
+
+// ----------------------------------------------------------------------------
+// host side
+// ----------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static std::mutex g_mu;
+static EncodeTiledFn g_encode = nullptr;
+static int g_avail = -1;
+
+static EncodeTiledFn encode_fn() {
+    std::lock_guard<std::mutex> g(g_mu);
+    if (!g_encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = (EncodeTiledFn)fn;
+        else
+            cudaGetLastError();
+    }
+    return g_encode;
+}
+
+static int make_map(CUtensorMap* map, void* base, uint64_t inner, uint64_t outer, uint32_t box_inner,
+                    uint32_t box_outer) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) { set_error("cuTensorMapEncodeTiled is not available"); return LNC_ERR_UNSUPPORTED; }
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {inner * 2};
+    cuuint32_t box[2] = {box_inner, box_outer};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return LNC_ERR_CUDA;
+    }
+    return LNC_OK;
+}
+
+static int m_pad_of(int64_t m) { return (int)((m + BM - 1) / BM * BM); }
+static int n_tiles_of(int64_t n) { return (int)((n + BN - 1) / BN); }
+
+}  // namespace tc
+
+bool trailing_tc_u32_available() {
+    using namespace tc;
+    if (g_avail >= 0) return g_avail == 1;
+    int ok = 0;
+    const char* env = getenv("LNC_DISABLE_TC");
+    if (!(env && env[0] == '1')) {
+        DeviceInfo di;
+        if (device_info(&di) == LNC_OK && di.cc_major == 10 && di.smem_optin >= (int)SMEM_BYTES &&
+            encode_fn() != nullptr)
+            ok = 1;
+    }
+    g_avail = ok;
+    return ok == 1;
+}
+
+size_t trailing_tc_u32_scratch(int64_t m, int64_t n, int /*b*/) {
+    using namespace tc;
+    const size_t el = (size_t)LIMBS * m_pad_of(m) * KMAX * 2;
+    const size_t bs = (size_t)n_tiles_of(n) * B_ROWS * KMAX * 2;
+    return ((el + 1023) / 1024 * 1024) + ((bs + 1023) / 1024 * 1024) + 1024;
+}
+
 int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s) {
-    return trailing_update_simt<FieldU32>(t, s);
+    using namespace tc;
+    const int m_pad = m_pad_of(t.m);
+    const int n_tiles = n_tiles_of(t.N);
+    const int n_tiles_max = n_tiles_of(t.n);
+    unsigned char* base = (unsigned char*)(((uintptr_t)t.extra + 1023) & ~(uintptr_t)1023);
+    __nv_bfloat16* EL = (__nv_bfloat16*)base;
+    const size_t el_bytes = ((size_t)LIMBS * m_pad * KMAX * 2 + 1023) / 1024 * 1024;
+    __nv_bfloat16* BS = (__nv_bfloat16*)(base + el_bytes);
+
+    CUtensorMap mapA, mapB;
+    int rc = make_map(&mapA, EL, KMAX, (uint64_t)LIMBS * m_pad, KC, BM);
+    if (rc) return rc;
+    rc = make_map(&mapB, BS, KMAX, (uint64_t)n_tiles_max * B_ROWS, KC, B_ROWS);
+    if (rc) return rc;
+
+    const uint32_t p = t.f.p;
+    {
+        const int64_t total = (int64_t)m_pad * KMAX;
+        const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
+        split_e_kernel<<<grid, 256, 0, s>>>(t.E, t.ldE, t.b, t.m, m_pad, p, t.panel_k, EL);
+        LNC_CHECK_LAUNCH("split_e_kernel");
+        gather_split_b_kernel<<<n_tiles, 256, 0, s>>>(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, p, BS);
+        LNC_CHECK_LAUNCH("gather_split_b_kernel");
+    }
+    TcParams P;
+    P.C = t.A + t.j1;
+    P.ldc = t.lda;
+    P.m = t.m;
+    P.N = t.N;
+    P.m_pad = m_pad;
+    P.n_tiles = n_tiles;
+    P.panel_k = t.panel_k;
+    P.f = t.f;
+    uint64_t w = 1 % p;
+    for (int sgrp = 0; sgrp < GROUPS; ++sgrp) {
+        P.w[sgrp] = (w > p / 2) ? (int32_t)((int64_t)w - (int64_t)p) : (int32_t)w;
+        w = (w * 256) % p;
+    }
+    P.off = ((((uint64_t)1 << 59) + p - 1) / p) * p;
+    P.err = t.err;
+    P.status = t.status;
+    LNC_CUDA(cudaFuncSetAttribute(limb_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+    dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
+    if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }
+    ScopedKernelTimer kt(KC_TRAILING, s);
+    limb_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(mapA, mapB, P);
+    LNC_CHECK_LAUNCH("limb_gemm_kernel");
+    return LNC_OK;
 }
 
 }  // namespace lnc

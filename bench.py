@@ -263,6 +263,8 @@ def run_ours(args, dist: Dist):
     lat = [a.elapsed_ms(b) for a, b in ev]
     kt = {name: _lib.kernel_timing_read(kc) for name, kc in
           (("panel", _lib.KC_PANEL), ("trailing", _lib.KC_TRAILING), ("gather", _lib.KC_GATHER))}
+    kt_work = {name: _lib.kernel_timing_work(kc) for name, kc in
+               (("panel", _lib.KC_PANEL), ("trailing", _lib.KC_TRAILING), ("gather", _lib.KC_GATHER))}
     _lib.kernel_timing(False)
     _lib.device_status()
 
@@ -294,32 +296,34 @@ def run_ours(args, dist: Dist):
     peaks = measured_peaks()
     W = rref_work(m, n, range(n)) if ident_ok else rref_work(m, n, piv[piv >= 0])
     dom = max(("panel", "trailing"), key=lambda k: kt[k][1])
-    L_limbs = 4
-    if dom == "trailing" and not (args.flags & _lib.LNC_FLAG_SIMT_TRAILING):
-        # tensor-core limb GEMM: 2 * L^2 bf16 flops per field multiply-add of the
-        # trailing updates; the trailing updates do W minus the panels' share
-        b = 128
-        w_trailing = trailing_work(m, n, b)
-        flops_per_launch = 2.0 * L_limbs * L_limbs * w_trailing / max(1, n // b)
-        per_launch_ms = kt["trailing"][1] / max(1, kt["trailing"][0])
-        achieved = flops_per_launch / (per_launch_ms / 1e3) / 1e12
-        peak = peaks["bf16_tflops_sustained"]
-        roof = {"bound": "tensor", "kernel": "trailing_update_tc", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic_per_launch("trailing"),
-                "peak_source": f"{peaks['source']} bf16 sustained",
-                "work_unit": "2*16 bf16 flops per F_p multiply-add (4 limbs x 4 limbs)"}
-    else:
-        kname = dom
-        if dom == "trailing":
-            bytes_per_launch = trailing_bytes(m, n, 128) / max(1, n // 128)
+    work = kt_work[dom]
+    if dom == "trailing":
+        if args.flags & _lib.LNC_FLAG_SIMT_TRAILING:
+            # SIMT integer contraction: report its HBM traffic against the copy roofline
+            launches = max(1, kt["trailing"][0])
+            bytes_per_launch = trailing_bytes(m, n, 128) / launches
+            achieved = trailing_bytes(m, n, 128) / (kt["trailing"][1] / 1e3) / 1e9
+            roof = {"bound": "hbm", "kernel": "trailing_simt_kernel", "achieved": achieved,
+                    "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                    "traffic": traffic_per_launch("trailing_simt"),
+                    "peak_source": f"{peaks['source']} copy bandwidth",
+                    "bytes_per_launch": bytes_per_launch}
         else:
-            bytes_per_launch = 2.0 * m * 128 * 4
-        per_launch_ms = kt[dom][1] / max(1, kt[dom][0])
-        achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
-        peak = peaks["hbm_gbs"]
-        roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic_per_launch(dom),
-                "peak_source": f"{peaks['source']} copy bandwidth"}
+            # tensor-core limb GEMM: 2 * L^2 bf16 flops per field multiply-add (L = 4 digits)
+            flops = 2.0 * 16.0 * work
+            achieved = flops / (kt["trailing"][1] / 1e3) / 1e12
+            peak = peaks["bf16_tflops_sustained"]
+            roof = {"bound": "tensor", "kernel": "tc::limb_gemm_kernel", "achieved": achieved, "peak": peak,
+                    "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic_per_launch("limb_gemm"),
+                    "peak_source": f"{peaks['source']} bf16 sustained (kernel timed inside a long solve)",
+                    "work_unit": "field multiply-adds m*N*128 per launch, x 2*4*4 bf16 flops",
+                    "flops_per_launch": flops / max(1, kt["trailing"][0])}
+    else:
+        achieved = work / (kt["panel"][1] / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": "panel (cand_panel_kernel / panel_kernel)", "achieved": achieved,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                "traffic": traffic_per_launch("panel"), "peak_source": f"{peaks['source']} copy bandwidth",
+                "note": "latency-bound: one pivot step per column"}
 
     line = {
         "metric": METRIC,
@@ -337,6 +341,8 @@ def run_ours(args, dist: Dist):
         "config": {"workload": f"rref_u32_{m}x{n}_p2^31-1", "m": m, "n": n, "p": p,
                    "parallelism": f"replicas x{dist.world}", "panel_width": 128,
                    "trailing": "simt" if args.flags & _lib.LNC_FLAG_SIMT_TRAILING else "tensor_core",
+                   "panel": "exhaustive" if args.flags & (_lib.LNC_FLAG_ROBUST_PANEL | _lib.LNC_FLAG_SIMT_TRAILING)
+                   else "candidate block + exhaustive fallback",
                    "l2": "input 1.6 GB > L2 (129 MB); no flush needed"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "min": float(min(lat)), "max": float(max(lat))},
@@ -344,7 +350,7 @@ def run_ours(args, dist: Dist):
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes + 8 * (kmax + 1), "call": "linac_gb300.cuda_row_reduce"},
         "gpu_launches": launches,
-        "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in kt.items()},
+        "kernel_ms": {k: {"launches": v[0], "total_ms": v[1], "work": kt_work[k]} for k, v in kt.items()},
         "roofline": roof,
         "clocks": clk.summary(),
         "host_wall_s": t_host,
@@ -444,6 +450,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rref_u32_20000")
     ap.add_argument("--simt", action="store_true", help="force the SIMT trailing update")
+    ap.add_argument("--robust-panel", action="store_true", help="force the exhaustive grid-wide panel")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--ref-seconds", type=float, default=6.0)
@@ -457,7 +464,8 @@ def main():
         line = run_reference(args, dist)
     else:
         from linac_gb300 import _lib  # fails loudly if the library is missing
-        args.flags = _lib.LNC_FLAG_SIMT_TRAILING if args.simt else 0
+        args.flags = (_lib.LNC_FLAG_SIMT_TRAILING if args.simt else 0) | \
+            (_lib.LNC_FLAG_ROBUST_PANEL if args.robust_panel else 0)
         line = run_ours(args, dist)
     if dist.rank == 0 and line is not None:
         print(json.dumps(line), flush=True)

@@ -44,6 +44,7 @@ extern "C" {
 #define LNC_FLAG_NONE 0
 #define LNC_FLAG_NO_SCALING 1   /* float path: skip the row pre-scaling     */
 #define LNC_FLAG_SIMT_TRAILING 2 /* force the SIMT trailing update (tests)  */
+#define LNC_FLAG_ROBUST_PANEL 4  /* F_p: always use the exhaustive grid-wide panel */
 
 /* ---- library / device ---------------------------------------------------- */
 /* Version string of the library. */
@@ -89,6 +90,10 @@ int lnc_kernel_timing_reset(void);
 /* Total launches and summed event time (ms) of one class since the reset;
  * synchronises the events it reads. */
 int lnc_kernel_timing_read(int kernel_class, int64_t* launches, double* total_ms);
+/* Algorithmic work of the timed launches of one class since the reset:
+ * field multiply-adds (trailing update, nominal contraction depth 128 per
+ * panel), bytes moved (panel, loader, gather). */
+int lnc_kernel_timing_work(int kernel_class, double* work);
 
 /* ---- RREF ------------------------------------------------------------------ */
 /*

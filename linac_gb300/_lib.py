@@ -32,6 +32,7 @@ DTYPE_CODE = {np.dtype(np.uint32): LNC_U32, np.dtype(np.uint64): LNC_U64,
 LNC_FLAG_NONE = 0
 LNC_FLAG_NO_SCALING = 1
 LNC_FLAG_SIMT_TRAILING = 2
+LNC_FLAG_ROBUST_PANEL = 4
 
 KC_PANEL, KC_TRAILING, KC_LOADER, KC_GATHER, KC_BATCH = 0, 1, 2, 3, 4
 
@@ -89,6 +90,7 @@ _SIGNATURES = {
     "lnc_kernel_timing_enable": ([_int], _int),
     "lnc_kernel_timing_reset": ([], _int),
     "lnc_kernel_timing_read": ([_int, _vp, _vp], _int),
+    "lnc_kernel_timing_work": ([_int, _vp], _int),
     "lnc_rref_host": ([_int, _i64, _i64, _u64, _dbl, _vp, _i64, _vp, _i64, _vp, _vp, _int], _int),
     "lnc_rref_device": ([_int, _i64, _i64, _u64, _dbl, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _int], _int),
     "lnc_load_matrix_host": ([_int, _i64, _i64, _i64, _i64, _u64, _vp, _vp, _vp], _int),
@@ -288,6 +290,12 @@ def kernel_timing_read(kclass: int):
     ms = ctypes.c_double()
     check(lib().lnc_kernel_timing_read(int(kclass), ctypes.byref(n), ctypes.byref(ms)))
     return int(n.value), float(ms.value)
+
+
+def kernel_timing_work(kclass: int) -> float:
+    w = ctypes.c_double()
+    check(lib().lnc_kernel_timing_work(int(kclass), ctypes.byref(w)))
+    return float(w.value)
 
 
 def device_info():

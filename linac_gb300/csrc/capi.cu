@@ -38,7 +38,12 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 // ---- kernel timing ---------------------------------------------------------
 static std::mutex g_timing_mu;
 static bool g_timing_enabled = false;
-static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_timing_pending[KC_COUNT];
+struct PendingTiming {
+    cudaEvent_t start, stop;
+    double work;
+};
+static std::vector<PendingTiming> g_timing_pending[KC_COUNT];
+static double g_timing_work[KC_COUNT];
 static std::vector<cudaEvent_t> g_event_pool;
 static int64_t g_timing_launches[KC_COUNT];
 static double g_timing_ms[KC_COUNT];
@@ -54,7 +59,7 @@ static cudaEvent_t pool_event() {
     return e;
 }
 
-ScopedKernelTimer::ScopedKernelTimer(int kc, cudaStream_t s) : kclass(kc), stream(s) {
+ScopedKernelTimer::ScopedKernelTimer(int kc, cudaStream_t s, double w) : kclass(kc), stream(s), work(w) {
     std::lock_guard<std::mutex> g(g_timing_mu);
     if (!g_timing_enabled) return;
     start = pool_event();
@@ -66,20 +71,21 @@ ScopedKernelTimer::~ScopedKernelTimer() {
     if (!start) return;
     std::lock_guard<std::mutex> g(g_timing_mu);
     cudaEventRecord(stop, stream);
-    g_timing_pending[kclass].push_back({start, stop});
+    g_timing_pending[kclass].push_back({start, stop, work});
 }
 
 static void timing_drain_locked() {
     for (int k = 0; k < KC_COUNT; ++k) {
         for (auto& pr : g_timing_pending[k]) {
-            cudaEventSynchronize(pr.second);
+            cudaEventSynchronize(pr.stop);
             float ms = 0.f;
-            if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) {
+            if (cudaEventElapsedTime(&ms, pr.start, pr.stop) == cudaSuccess) {
                 g_timing_ms[k] += ms;
                 g_timing_launches[k] += 1;
+                g_timing_work[k] += pr.work;
             }
-            g_event_pool.push_back(pr.first);
-            g_event_pool.push_back(pr.second);
+            g_event_pool.push_back(pr.start);
+            g_event_pool.push_back(pr.stop);
         }
         g_timing_pending[k].clear();
     }
@@ -317,7 +323,7 @@ int lnc_kernel_timing_enable(int enable) {
 int lnc_kernel_timing_reset(void) {
     std::lock_guard<std::mutex> g(g_timing_mu);
     timing_drain_locked();
-    for (int k = 0; k < KC_COUNT; ++k) { g_timing_ms[k] = 0.0; g_timing_launches[k] = 0; }
+    for (int k = 0; k < KC_COUNT; ++k) { g_timing_ms[k] = 0.0; g_timing_launches[k] = 0; g_timing_work[k] = 0.0; }
     return LNC_OK;
 }
 
@@ -327,6 +333,14 @@ int lnc_kernel_timing_read(int kc, int64_t* launches, double* total_ms) {
     timing_drain_locked();
     if (launches) *launches = g_timing_launches[kc];
     if (total_ms) *total_ms = g_timing_ms[kc];
+    return LNC_OK;
+}
+
+int lnc_kernel_timing_work(int kc, double* work) {
+    if (kc < 0 || kc >= KC_COUNT) { set_error("unknown kernel class %d", kc); return LNC_ERR_INVALID; }
+    std::lock_guard<std::mutex> g(g_timing_mu);
+    timing_drain_locked();
+    if (work) *work = g_timing_work[kc];
     return LNC_OK;
 }
 

@@ -42,11 +42,15 @@ enum KernelClass : int {
     KC_COUNT = 5
 };
 
+// Records CUDA events around one launch of a kernel class (when timing is
+// enabled) together with the launch's algorithmic work (units chosen per
+// class: field multiply-adds for the trailing update, bytes for the others).
 struct ScopedKernelTimer {
-    ScopedKernelTimer(int kclass, cudaStream_t s);
+    ScopedKernelTimer(int kclass, cudaStream_t s, double work = 0.0);
     ~ScopedKernelTimer();
     int kclass;
     cudaStream_t stream;
+    double work;
     cudaEvent_t start = nullptr, stop = nullptr;
 };
 

@@ -187,7 +187,9 @@ static int launch_loader(const Ops& ops, int64_t n_rows, int64_t n_cols, int64_t
     const int64_t gy = (n_rows + kLoadRows - 1) / kLoadRows;
     const int64_t gx = (n_cols + kLoadCols - 1) / kLoadCols;
     if (gy > 65535 || gx > 2147483647ll) { set_error("loader: matrix too large"); return LNC_ERR_UNSUPPORTED; }
-    ScopedKernelTimer kt(KC_LOADER, s);
+    ScopedKernelTimer kt(KC_LOADER, s,
+                         (double)sizeof(T) * ((double)n_rows * n_cols + (double)n_rows * basis_len) +
+                             4.0 * (double)n_cols * degree);
     kern<<<dim3((unsigned)gx, (unsigned)gy), kLoadCols, smem, s>>>(ops, (const T*)bases, n_rows, basis_len, lind,
                                                                    n_cols, (int)degree, (T*)out, ldo);
     LNC_CHECK_LAUNCH("load_matrix_kernel");

@@ -151,6 +151,10 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_kernel(PanelArgs<F> a)
     __shared__ T s_inv;
 
     if (ld_volatile_i32(a.bar.err) != 0) return;
+    if (a.run_if != nullptr && ld_volatile_i32(a.run_if) == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *a.panel_k = 0;
+        return;
+    }
     const int64_t rank0 = *a.rank;
 
     for (int r = warp; r < R; r += NW) {
@@ -466,6 +470,57 @@ int plan_rref(int64_t m, int64_t n, RrefPlan* plan) {
     return LNC_OK;
 }
 
+// scratch of the candidate-panel path (32-bit residues)
+static size_t fast_extra_scratch(int64_t m, int64_t n) {
+    return align_up(sizeof(uint32_t) * kMaxPanel * kMaxPanel, 256)  // X
+           + align_up(sizeof(int32_t) * 256, 256)                     // candidate rows
+           + 256                                                      // cand_n, next_row, missed, pivmask
+           + align_up(sizeof(int32_t) * kMaxPanel, 256)               // panel_cols
+           + align_up(sizeof(int32_t) * (size_t)m, 256)               // panel_mark
+           + align_up(sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1), 256);  // column -> pivot row
+}
+
+// Pivots may be found out of column order when a candidate panel is redone by
+// the exhaustive panel: order the (row, column) lists by column (one CTA).
+__global__ void __launch_bounds__(1024) sort_pivots_kernel(int32_t* piv_row, int64_t* piv_col, const int64_t* rank_p,
+                                                           int64_t n, int32_t* col_row) {
+    __shared__ int s_warp[32];
+    __shared__ int s_base, s_total;
+    const int64_t rank = *rank_p;
+    for (int64_t c = threadIdx.x; c < n; c += blockDim.x) col_row[c] = -1;
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < rank; i += blockDim.x) col_row[piv_col[i]] = piv_row[i];
+    if (threadIdx.x == 0) s_base = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int64_t c0 = 0; c0 < n; c0 += blockDim.x) {
+        const int64_t c = c0 + threadIdx.x;
+        const int32_t r = (c < n) ? col_row[c] : -1;
+        const int flag = r >= 0;
+        const unsigned ballot = __ballot_sync(0xffffffffu, flag);
+        if (lane == 0) s_warp[warp] = __popc(ballot);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                const int v = s_warp[w];
+                s_warp[w] = acc;
+                acc += v;
+            }
+            s_total = acc;
+        }
+        __syncthreads();
+        const int pos = s_base + s_warp[warp] + __popc(ballot & ((1u << lane) - 1u));
+        if (flag) {
+            piv_row[pos] = r;
+            piv_col[pos] = c;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_base += s_total;
+        __syncthreads();
+    }
+}
+
 template <class F>
 size_t rref_scratch_bytes(int64_t m, int64_t n, const RrefPlan& pl) {
     using T = typename F::T;
@@ -482,6 +537,7 @@ size_t rref_scratch_bytes(int64_t m, int64_t n, const RrefPlan& pl) {
     s += align_up(sizeof(T) * (size_t)m * pl.b, 256);           // E
     s += align_up(sizeof(T) * (size_t)pl.b * (size_t)std::max<int64_t>(n, 1), 256);  // Bm
     s += trailing_extra_scratch<F>(m, n, pl);
+    if constexpr (F::kDtype == 1) s += fast_extra_scratch(m, n);
     return s;
 }
 
@@ -555,10 +611,7 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
     tctx.b = pl.b;
     tctx.force_simt = (flags & LNC_FLAG_SIMT_TRAILING) != 0;
 
-    for (int64_t j0 = 0; j0 < n; j0 += pl.b) {
-        const int bw = (int)std::min<int64_t>(pl.b, n - j0);
-        const int64_t j1 = j0 + bw;
-        const int64_t N = n - j1;
+    auto make_panel_args = [&](int64_t j0, int bw, bool with_e, const int* run_if) {
         PanelArgs<F> pa;
         pa.f = f;
         pa.A = A;
@@ -573,7 +626,7 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
         pa.piv_col = piv_col;
         pa.panel_k = panel_k;
         pa.panel_rows = panel_rows;
-        pa.E = (N > 0) ? E : nullptr;
+        pa.E = with_e ? E : nullptr;
         pa.ldE = pl.b;
         pa.cand_key = cand_key;
         pa.cand_row = cand_row;
@@ -583,24 +636,131 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
         pa.bar.err = err;
         pa.bar.status = status;
         pa.rows_per_cta = pl.rows_per_cta;
-        {
-            ScopedKernelTimer kt(KC_PANEL, s);
-            void* args[] = {&pa};
-            const size_t smem = panel_smem_bytes<F>(pl.rows_per_cta, bw);
-            LNC_CUDA(cudaLaunchCooperativeKernel((const void*)kpanel, dim3(pl.G), dim3(kPanelThreads), args,
-                                                 smem, s));
-            LNC_CHECK_LAUNCH("panel_kernel");
+        pa.run_if = run_if;
+        return pa;
+    };
+    auto launch_panel = [&](PanelArgs<F>& pa) -> int {
+        ScopedKernelTimer kt(KC_PANEL, s, pa.run_if ? 0.0 : 2.0 * (double)m * pa.bw * sizeof(T));
+        void* args[] = {&pa};
+        const size_t smem = panel_smem_bytes<F>(pl.rows_per_cta, pa.bw);
+        LNC_CUDA(cudaLaunchCooperativeKernel((const void*)kpanel, dim3(pl.G), dim3(kPanelThreads), args, smem, s));
+        LNC_CHECK_LAUNCH("panel_kernel");
+        return LNC_OK;
+    };
+
+    bool fast = false;
+    if constexpr (F::kDtype == 1) {
+        fast = !(flags & (LNC_FLAG_SIMT_TRAILING | LNC_FLAG_ROBUST_PANEL)) && pl.b == kMaxPanel &&
+               trailing_tc_u32_available();
+    }
+    if (fast) {
+        if constexpr (F::kDtype == 1) {
+            // ---------------- candidate-block panels + tensor-core updates
+            unsigned char* fx = (unsigned char*)extra + trailing_extra_scratch<F>(m, n, pl);
+            fx = (unsigned char*)(((uintptr_t)fx + 255) & ~(uintptr_t)255);
+            auto takef = [&](size_t bytes) { void* r = fx; fx += align_up(bytes, 256); return r; };
+            uint32_t* Xbuf = (uint32_t*)takef(sizeof(uint32_t) * kMaxPanel * kMaxPanel);
+            int32_t* cand = (int32_t*)takef(sizeof(int32_t) * 256);
+            unsigned char* fscal = (unsigned char*)takef(256);
+            int32_t* cand_n = (int32_t*)fscal;
+            int32_t* next_row = (int32_t*)(fscal + 4);
+            int* missed = (int*)(fscal + 8);
+            uint32_t* pivmask = (uint32_t*)(fscal + 16);
+            int32_t* panel_cols = (int32_t*)takef(sizeof(int32_t) * kMaxPanel);
+            int32_t* panel_mark = (int32_t*)takef(sizeof(int32_t) * (size_t)m);
+            int32_t* col_row = (int32_t*)takef(sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1));
+            if ((size_t)(fx - (unsigned char*)scratch) > scratch_bytes) {
+                set_error("internal: scratch layout overflow (fast path)");
+                return LNC_ERR_INVALID;
+            }
+            LNC_CUDA(cudaMemsetAsync(fscal, 0, 256, s));
+            LNC_CUDA(cudaMemsetAsync(panel_mark, 0, sizeof(int32_t) * (size_t)m, s));
+            unsigned char* tcb = (unsigned char*)(((uintptr_t)extra + 1023) & ~(uintptr_t)1023);
+            void* EL = tcb;
+            void* BS = tcb + tc_el_bytes(m);
+            CandArgs ca;
+            ca.A = A;
+            ca.lda = lda;
+            ca.m = m;
+            ca.smax = kCandRows;
+            ca.row_used = row_used;
+            ca.cand = cand;
+            ca.cand_n = cand_n;
+            ca.next_row = next_row;
+            ca.rank = rank;
+            ca.piv_row = piv_row;
+            ca.piv_col = piv_col;
+            ca.panel_k = panel_k;
+            ca.panel_rows = panel_rows;
+            ca.panel_cols = panel_cols;
+            ca.panel_mark = panel_mark;
+            ca.X = Xbuf;
+            ca.pivmask = pivmask;
+            ca.missed = missed;
+            {
+                const uint32_t pp = f.p;
+                uint32_t x = pp;
+                for (int i = 0; i < 5; ++i) x *= 2u - pp * x;
+                ca.M.p = pp;
+                ca.M.pinv = 0u - x;
+                ca.M.r2 = (uint32_t)((((unsigned __int128)1) << 64) % pp);
+                ca.M.mu = f.mu;
+            }
+            int gen = 0;
+            for (int64_t j0 = 0; j0 < n; j0 += pl.b) {
+                const int bw = (int)std::min<int64_t>(pl.b, n - j0);
+                const int64_t j1 = j0 + bw;
+                ++gen;
+                ca.j0 = j0;
+                ca.bw = bw;
+                ca.gen = gen;
+                int rc = launch_cand_panel(ca, s);
+                if (!rc) rc = launch_split_g(A, lda, m, j0, f.p, panel_k, panel_cols, panel_mark, gen, EL, s);
+                // E = G X  (m x 128, overwritten)
+                if (!rc) rc = tc_gather_split_b(Xbuf, kMaxPanel, kMaxPanel, nullptr, panel_k, f.p, BS, false, s);
+                if (!rc) rc = tc_limb_gemm(f, E, kMaxPanel, m, kMaxPanel, panel_k, true, EL, BS, n, err, status, s);
+                // A[:, j0:] += E A[P, j0:]  (pivot rows zeroed first)
+                if (!rc) rc = tc_split_e(E, kMaxPanel, kMaxPanel, m, f.p, panel_k, EL, s);
+                if (!rc) rc = tc_gather_split_b(A + j0, lda, n - j0, panel_rows, panel_k, f.p, BS, true, s);
+                if (!rc) rc = tc_limb_gemm(f, A + j0, lda, m, n - j0, panel_k, false, EL, BS, n, err, status, s);
+                if (!rc) rc = launch_check_missed(A, lda, m, j0, bw, row_used, pivmask, missed, s);
+                if (rc) return rc;
+                // redo the panel exhaustively when the candidate block missed a pivot
+                PanelArgs<F> pa = make_panel_args(j0, bw, j1 < n, missed);
+                rc = launch_panel(pa);
+                if (rc) return rc;
+                if (j1 < n) {
+                    tctx.j1 = j1;
+                    tctx.N = n - j1;
+                    tctx.ldb = n - j1;
+                    tctx.predicated = true;
+                    rc = trailing_update<F>(tctx, s);
+                    tctx.predicated = false;
+                    if (rc) return rc;
+                }
+            }
+            sort_pivots_kernel<<<1, 1024, 0, s>>>(piv_row, piv_col, rank, n, col_row);
+            LNC_CHECK_LAUNCH("sort_pivots_kernel");
         }
-        if (N > 0) {
-            tctx.j1 = j1;
-            tctx.N = N;
-            tctx.ldb = N;
-            int rc = trailing_update<F>(tctx, s);
+    } else {
+        for (int64_t j0 = 0; j0 < n; j0 += pl.b) {
+            const int bw = (int)std::min<int64_t>(pl.b, n - j0);
+            const int64_t j1 = j0 + bw;
+            const int64_t N = n - j1;
+            PanelArgs<F> pa = make_panel_args(j0, bw, N > 0, nullptr);
+            int rc = launch_panel(pa);
             if (rc) return rc;
+            if (N > 0) {
+                tctx.j1 = j1;
+                tctx.N = N;
+                tctx.ldb = N;
+                rc = trailing_update<F>(tctx, s);
+                if (rc) return rc;
+            }
         }
     }
     {
-        ScopedKernelTimer kt(KC_GATHER, s);
+        ScopedKernelTimer kt(KC_GATHER, s, 2.0 * (double)m * (double)n * sizeof(T));
         dim3 grid((unsigned)std::min<int64_t>((n + 255) / 256, 16), (unsigned)std::min<int64_t>(m, 65535));
         T zero;
         memset(&zero, 0, sizeof(T));
@@ -630,7 +790,7 @@ int trailing_update_simt(const TrailingCtx<F>& t, cudaStream_t s) {
     }
     dim3 grid((unsigned)((t.N + 127) / 128), (unsigned)((t.m + 63) / 64));
     if (grid.y > 65535) { set_error("trailing update: too many row tiles"); return LNC_ERR_UNSUPPORTED; }
-    ScopedKernelTimer kt(KC_TRAILING, s);
+    ScopedKernelTimer kt(KC_TRAILING, s, (double)t.m * (double)t.N * (double)t.b);
     if constexpr (F::kDtype == 1) {
         if (t.f.p < (1u << 31))
             trailing_simt_kernel<F, 32, 4><<<grid, 256, 0, s>>>(t.f, t.A, t.lda, t.m, t.j1, t.N, t.E, t.ldE, t.Bm, t.ldb, t.panel_k);

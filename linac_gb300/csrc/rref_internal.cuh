@@ -39,6 +39,7 @@ struct PanelArgs {
     typename F::T* cand_vals;   // [2][G][b] proposed rows
     GridBarrier bar;
     int rows_per_cta;
+    const int* run_if;      // optional: the kernel does nothing unless *run_if != 0
 };
 
 // Multiply-accumulate policy of the SIMT trailing update, per field.
@@ -135,6 +136,7 @@ struct TrailingCtx {
     int b = 0;
     int64_t j1 = 0, N = 0;             // trailing columns [j1, j1 + N)
     bool force_simt = false;
+    bool predicated = false;           // runs only if the panel before it found pivots (fallback)
 };
 
 template <class F>
@@ -144,6 +146,58 @@ int trailing_update_simt(const TrailingCtx<F>& t, cudaStream_t s);
 int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s);
 size_t trailing_tc_u32_scratch(int64_t m, int64_t n, int b);
 bool trailing_tc_u32_available();
+
+// Reusable tensor-core pieces (trailing_tc.cu)
+size_t tc_el_bytes(int64_t m);
+size_t tc_bs_bytes(int64_t n);
+int tc_m_pad(int64_t m);
+int tc_split_e(const uint32_t* E, int64_t ldE, int b, int64_t m, uint32_t p, const int32_t* k_ptr, void* EL,
+               cudaStream_t s);
+int tc_gather_split_b(uint32_t* C, int64_t ldc, int64_t N, const int32_t* rows, const int32_t* k_ptr, uint32_t p,
+                      void* BS, bool zero_src, cudaStream_t s);
+int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t N, const int32_t* k_ptr,
+                 bool overwrite, const void* EL, const void* BS, int64_t n_map, int* err, int* status,
+                 cudaStream_t s, bool count_work = true);
+
+// Candidate-block panel for F_p with 32-bit residues (cand_panel.cu)
+constexpr int kCandThreads = 512;
+constexpr int kCandRows = 160;  // candidate rows per panel (panel width + 32)
+struct CandMont {
+    uint32_t p, pinv, r2;
+    uint64_t mu;
+};
+struct CandArgs {
+    const uint32_t* A;
+    int64_t lda;
+    int64_t m;
+    int64_t j0;
+    int bw;
+    int smax;
+    uint8_t* row_used;
+    int32_t* cand;      // [256] current candidate rows
+    int32_t* cand_n;
+    int32_t* next_row;  // rows >= next_row have not been candidates yet
+    int64_t* rank;
+    int32_t* piv_row;
+    int64_t* piv_col;
+    int32_t* panel_k;
+    int32_t* panel_rows;
+    int32_t* panel_cols;
+    int32_t* panel_mark;  // (gen << 8) | (t + 1) for the pivot rows of panel `gen`
+    int gen;
+    uint32_t* X;          // [kMaxPanel][kMaxPanel] inverse of the pivot block
+    uint32_t* pivmask;    // [4] pivot columns of the panel
+    int* missed;
+    struct {
+        uint32_t p, pinv, r2;
+        uint64_t mu;
+    } M;
+};
+int launch_cand_panel(const CandArgs& a, cudaStream_t s);
+int launch_split_g(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, uint32_t p, const int32_t* panel_k,
+                   const int32_t* panel_cols, const int32_t* panel_mark, int gen, void* EL, cudaStream_t s);
+int launch_check_missed(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, int bw, const uint8_t* row_used,
+                        const uint32_t* pivmask, int* missed, cudaStream_t s);
 
 template <class F>
 inline size_t trailing_extra_scratch(int64_t m, int64_t n, const RrefPlan& pl) {

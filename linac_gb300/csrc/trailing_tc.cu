@@ -42,21 +42,26 @@ namespace lnc {
 namespace tc {
 
 constexpr int BM = 128;                 // tile rows (TMEM lanes)
-constexpr int BN = 64;                  // output columns per tile
+constexpr int BN = 32;                  // output columns per tile
 constexpr int LIMBS = 4;                // base-256 digits per residue
 constexpr int KMAX = 128;               // contraction depth (panel width)
 constexpr int KC = 64;                  // K per stage: one 128-byte swizzle row of BF16
 constexpr int NKC = KMAX / KC;          // 2
 constexpr int GROUPS = 2 * LIMBS - 1;   // 7 weights 256^0 .. 256^6
-constexpr int B_ROWS = LIMBS * BN;      // 256 stacked digit rows per output tile
-constexpr int STAGES = 2;
-constexpr int TILES_PER_CTA = 8;
-constexpr int THREADS = 192;
+constexpr int B_ROWS = LIMBS * BN;      // 128 stacked digit rows per output tile (UMMA N)
+constexpr int STAGES = 4;
+constexpr int TILES_PER_CTA = 16;
+constexpr int EPI_WARPS = 8;            // two per TMEM lane quarter, 16 columns each
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t ACC_STRIDE = 256;    // two accumulators of GROUPS * BN = 224 columns
 constexpr uint32_t A_TILE_BYTES = BM * KC * 2;      // 16 KB
-constexpr uint32_t B_TILE_BYTES = B_ROWS * KC * 2;  // 32 KB
+constexpr uint32_t B_TILE_BYTES = B_ROWS * KC * 2;  // 16 KB
 constexpr uint32_t A_BYTES = LIMBS * NKC * A_TILE_BYTES;  // 128 KB
 constexpr uint32_t SMEM_BYTES = A_BYTES + STAGES * B_TILE_BYTES + 1024 /*barriers*/ + 1024 /*align*/;
+// exact float -> int for |x| < 2^22: x + 1.5 * 2^23 has unit spacing
+constexpr float MAGIC_F = 12582912.0f;
+constexpr int32_t MAGIC_I = 0x4B400000;
 
 struct TcParams {
     uint32_t* C;            // trailing block base: A + j1
@@ -69,6 +74,7 @@ struct TcParams {
     FieldU32 f;
     int32_t w[GROUPS];      // 256^s mod p, centred
     uint64_t off;           // multiple of p >= 2^59 (makes the 64-bit sum non-negative)
+    int overwrite;          // 1: C <- E * B (C is not read), 0: C <- C + E * B
     int* err;
     int* status;
 };
@@ -108,7 +114,7 @@ __global__ void split_e_kernel(const uint32_t* E, int64_t ldE, int b, int64_t m,
 // tile), zeroing those rows in C.
 __global__ void __launch_bounds__(256) gather_split_b_kernel(uint32_t* C, int64_t ldc, int64_t N,
                                                              const int32_t* panel_rows, const int32_t* panel_k,
-                                                             uint32_t p, __nv_bfloat16* BS) {
+                                                             uint32_t p, __nv_bfloat16* BS, int zero_src) {
     __shared__ uint32_t s[KMAX][BN + 1];
     const int k = *panel_k;
     if (k == 0) return;
@@ -119,9 +125,9 @@ __global__ void __launch_bounds__(256) gather_split_b_kernel(uint32_t* C, int64_
         const int t = idx / BN, cc = idx % BN;
         uint32_t v = 0;
         if (t < k && c0 + cc < N) {
-            uint32_t* src = C + (int64_t)panel_rows[t] * ldc + c0 + cc;
+            uint32_t* src = C + (int64_t)(panel_rows ? panel_rows[t] : t) * ldc + c0 + cc;
             v = *src;
-            *src = 0u;
+            if (zero_src) *src = 0u;
         }
         s[t][cc] = v;
     }
@@ -153,12 +159,12 @@ __global__ void __launch_bounds__(THREADS, 1)
     unsigned char* sB = smem + A_BYTES;               // [STAGES][B_ROWS x KC]
     uint64_t* bars = (uint64_t*)(sB + STAGES * B_TILE_BYTES);
     uint64_t* a_full = bars + 0;
-    uint64_t* b_full = bars + 1;   // [STAGES]
-    uint64_t* b_empty = bars + 3;  // [STAGES]
-    uint64_t* acc_full = bars + 5;
-    uint64_t* acc_empty = bars + 6;
-    uint64_t* drain = bars + 7;
-    uint32_t* s_tmem = (uint32_t*)(bars + 8);
+    uint64_t* b_full = bars + 1;                  // [STAGES]
+    uint64_t* b_empty = bars + 1 + STAGES;        // [STAGES]
+    uint64_t* acc_full = bars + 1 + 2 * STAGES;   // [2]
+    uint64_t* acc_empty = bars + 3 + 2 * STAGES;  // [2]
+    uint64_t* drain = bars + 5 + 2 * STAGES;
+    uint32_t* s_tmem = (uint32_t*)(bars + 6 + 2 * STAGES);
     __shared__ volatile int s_err;
 
     const int k = *P.panel_k;  // written by an earlier kernel: identical in every thread
@@ -177,8 +183,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             ptx::mbar_init(&b_full[s], 1);
             ptx::mbar_init(&b_empty[s], 1);
         }
-        ptx::mbar_init(acc_full, 1);
-        ptx::mbar_init(acc_empty, 4);
+        for (int b = 0; b < 2; ++b) {
+            ptx::mbar_init(&acc_full[b], 1);
+            ptx::mbar_init(&acc_empty[b], EPI_WARPS);
+        }
         ptx::mbar_init(drain, 1);
         ptx::fence_mbar_init();
     }
@@ -202,7 +210,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                     ptx::tma_load_2d(sA + (i * NKC + kc) * A_TILE_BYTES, &tmA, a_full, kc * KC,
                                      i * P.m_pad + rb * BM);
             int it = 0;
-            int issued_round[STAGES] = {-1, -1};
+            int issued_round[STAGES];
+            for (int st = 0; st < STAGES; ++st) issued_round[st] = -1;
             for (int t = 0; t < ntiles && !s_err; ++t) {
                 for (int kc = 0; kc < nkc; ++kc, ++it) {
                     const int st = it % STAGES, round = it / STAGES;
@@ -228,8 +237,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (!ok) flag_error(P, &s_err);
             int it = 0;
             for (int t = 0; t < ntiles && ok; ++t) {
-                if (!ptx::mbar_wait(acc_empty, t & 1, &s_err)) { flag_error(P, &s_err); break; }
+                const int buf = t & 1;
+                if (!ptx::mbar_wait(&acc_empty[buf], (t >> 1) & 1, &s_err)) { flag_error(P, &s_err); break; }
                 ptx::tc_fence_after();
+                const uint32_t dbase = tmem + ACC_STRIDE * buf;
                 for (int kc = 0; kc < nkc && ok; ++kc, ++it) {
                     const int st = it % STAGES, round = it / STAGES;
                     if (!ptx::mbar_wait(&b_full[st], round & 1, &s_err)) { flag_error(P, &s_err); ok = false; break; }
@@ -241,12 +252,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                         for (int i = 0; i < LIMBS; ++i) {
                             const uint64_t adesc =
                                 ptx::umma_desc_sw128(a_base + (i * NKC + kc) * A_TILE_BYTES + ks * 32);
-                            ptx::umma_bf16(tmem + 64u * i, adesc, bdesc, idesc, 1u);
+                            ptx::umma_bf16(dbase + (uint32_t)(BN * i), adesc, bdesc, idesc, 1u);
                         }
                     }
                     ptx::umma_commit(&b_empty[st]);  // stage reusable once these UMMAs finish
                 }
-                if (ok) ptx::umma_commit(acc_full);
+                if (ok) ptx::umma_commit(&acc_full[buf]);
             }
             // all issued UMMAs complete before the TMEM is released
             ptx::umma_commit(drain);
@@ -254,71 +265,105 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
     } else {
         // ------------------------------------------------------------ epilogue
-        const int q = warp & 3;  // TMEM lane quarter this warp may access
+        const int ew = warp - 2;            // 0 .. EPI_WARPS-1
+        const int q = warp & 3;             // TMEM lane quarter this warp may access
+        const int half = ew >> 2;           // which 16 of the tile's 32 columns
         const int64_t row = (int64_t)rb * BM + q * 32 + lane;
-        const uint32_t t_lane = tmem + ((uint32_t)(q * 32) << 16);
-        // zero the accumulator (this warp's 32 lanes, 7 x 64 columns)
-        for (int c = 0; c < GROUPS * BN; c += 16) ptx::tmem_st16_zero(t_lane + c);
+        const uint32_t t_lane = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(16 * half);
+        const FieldU32 f = P.f;
+        const bool row_ok = row < P.m;
+        // zero both accumulators (this warp's lanes and columns)
+        for (int b = 0; b < 2; ++b) {
+            for (int g = 0; g < GROUPS; ++g) ptx::tmem_st16_zero(t_lane + ACC_STRIDE * b + BN * g);
+        }
         ptx::tmem_st_wait();
         ptx::tc_fence_before();
         __syncwarp();
-        if (lane == 0) ptx::mbar_arrive(acc_empty);
-        const FieldU32 f = P.f;
-        for (int t = 0; t < ntiles; ++t) {
-            const int64_t col0 = (int64_t)(t0 + t) * BN;
-            const bool row_ok = row < P.m;
-            uint32_t* crow = P.C + (row_ok ? row : 0) * P.ldc + col0;
-            const int ncols = (int)((P.N - col0) < BN ? (P.N - col0) : BN);
-            uint32_t old[BN];
-            if (row_ok && ncols == BN && ((((uintptr_t)crow) & 15) == 0)) {
+        if (lane == 0) {
+            ptx::mbar_arrive(&acc_empty[0]);
+            ptx::mbar_arrive(&acc_empty[1]);
+        }
+        int64_t wsum = 0;  // sum of the weights: removes the magic offset in one step
 #pragma unroll
-                for (int c = 0; c < BN; c += 4) {
-                    uint4 v = *(const uint4*)(crow + c);
+        for (int g = 0; g < GROUPS; ++g) wsum += P.w[g];
+        const uint64_t bias = P.off - (uint64_t)((int64_t)MAGIC_I * wsum);
+        for (int t = 0; t < ntiles; ++t) {
+            const int buf = t & 1;
+            const int64_t col0 = (int64_t)(t0 + t) * BN + 16 * half;
+            uint32_t* crow = P.C + (row_ok ? row : 0) * P.ldc + col0;
+            const int ncols = (int)((P.N - col0) < 16 ? (P.N - col0) : 16);
+            const bool vec = row_ok && ncols == 16 && ((((uintptr_t)crow) & 15) == 0);
+            uint32_t old[16];
+            if (P.overwrite) {
+#pragma unroll
+                for (int c = 0; c < 16; ++c) old[c] = 0u;
+            } else if (vec) {
+#pragma unroll
+                for (int c = 0; c < 16; c += 4) {
+                    const uint4 v = *(const uint4*)(crow + c);
                     old[c] = v.x; old[c + 1] = v.y; old[c + 2] = v.z; old[c + 3] = v.w;
                 }
             } else {
 #pragma unroll
-                for (int c = 0; c < BN; ++c) old[c] = (row_ok && c < ncols) ? crow[c] : 0u;
+                for (int c = 0; c < 16; ++c) old[c] = (row_ok && c < ncols) ? crow[c] : 0u;
             }
-            const bool got = ptx::mbar_wait(acc_full, t & 1, &s_err);
+            const bool got = ptx::mbar_wait(&acc_full[buf], (t >> 1) & 1, &s_err);
             if (!__all_sync(0xffffffffu, got)) {  // warp-uniform before the aligned TMEM loads
                 if (lane == 0) flag_error(P, &s_err);
                 break;
             }
             ptx::tc_fence_after();
-            const bool vec = row_ok && ncols == BN && ((((uintptr_t)crow) & 15) == 0);
+            uint32_t d[GROUPS][16];
 #pragma unroll
-            for (int cb = 0; cb < BN / 16; ++cb) {
-                uint32_t d[GROUPS][16];
-#pragma unroll
-                for (int s = 0; s < GROUPS; ++s) ptx::tmem_ld16(t_lane + s * BN + cb * 16, d[s]);
-                ptx::tmem_ld_wait();
-                uint32_t res[16];
-#pragma unroll
-                for (int c = 0; c < 16; ++c) {
-                    int64_t v = 0;
-#pragma unroll
-                    for (int s = 0; s < GROUPS; ++s)
-                        v += (int64_t)__float2int_rn(__uint_as_float(d[s][c])) * (int64_t)P.w[s];
-                    const uint32_t r = f.reduce64((uint64_t)(v + (int64_t)P.off));
-                    res[c] = f.add(old[cb * 16 + c], r);
-                }
-                if (vec) {
-#pragma unroll
-                    for (int c = 0; c < 16; c += 4)
-                        *(uint4*)(crow + cb * 16 + c) = make_uint4(res[c], res[c + 1], res[c + 2], res[c + 3]);
-                } else if (row_ok) {
-#pragma unroll
-                    for (int c = 0; c < 16; ++c)
-                        if (cb * 16 + c < ncols) crow[cb * 16 + c] = res[c];
-                }
-            }
+            for (int g = 0; g < GROUPS; ++g) ptx::tmem_ld16(t_lane + ACC_STRIDE * buf + BN * g, d[g]);
+            ptx::tmem_ld_wait();
             // accumulator drained: re-zero it and hand it back to the MMA warp
-            for (int c = 0; c < GROUPS * BN; c += 16) ptx::tmem_st16_zero(t_lane + c);
+#pragma unroll
+            for (int g = 0; g < GROUPS; ++g) ptx::tmem_st16_zero(t_lane + ACC_STRIDE * buf + BN * g);
             ptx::tmem_st_wait();
             ptx::tc_fence_before();
             __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(acc_empty);
+            if (lane == 0) ptx::mbar_arrive(&acc_empty[buf]);
+            // exact conversion: for |x| < 2^22, x + 1.5 * 2^23 is exact and its bit pattern minus
+            // 0x4B400000 is x (full-rate FADD instead of the quarter-rate F2I); the weighted sum is
+            // formed modulo 2^64, its true value off + sum x_g w_g lies in [0, 2^60]
+            float mx = 0.f;
+#pragma unroll
+            for (int g = 0; g < GROUPS; ++g)
+#pragma unroll
+                for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
+            const bool fast = mx < 4194304.0f;
+            uint32_t res[16];
+            if (__all_sync(0xffffffffu, fast)) {
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    uint64_t v = (uint64_t)bias;
+#pragma unroll
+                    for (int g = 0; g < GROUPS; ++g) {
+                        const int32_t y = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F));
+                        v += (uint64_t)((int64_t)y * (int64_t)P.w[g]);
+                    }
+                    res[c] = f.add(old[c], f.reduce64(v));
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    uint64_t v = P.off;
+#pragma unroll
+                    for (int g = 0; g < GROUPS; ++g)
+                        v += (uint64_t)((int64_t)__float2int_rn(__uint_as_float(d[g][c])) * (int64_t)P.w[g]);
+                    res[c] = f.add(old[c], f.reduce64(v));
+                }
+            }
+            if (vec) {
+#pragma unroll
+                for (int c = 0; c < 16; c += 4)
+                    *(uint4*)(crow + c) = make_uint4(res[c], res[c + 1], res[c + 2], res[c + 3]);
+            } else if (row_ok) {
+#pragma unroll
+                for (int c = 0; c < 16; ++c)
+                    if (c < ncols) crow[c] = res[c];
+            }
         }
     }
     ptx::tc_fence_before();
@@ -393,60 +438,89 @@ bool trailing_tc_u32_available() {
 
 size_t trailing_tc_u32_scratch(int64_t m, int64_t n, int /*b*/) {
     using namespace tc;
-    const size_t el = (size_t)LIMBS * m_pad_of(m) * KMAX * 2;
-    const size_t bs = (size_t)n_tiles_of(n) * B_ROWS * KMAX * 2;
-    return ((el + 1023) / 1024 * 1024) + ((bs + 1023) / 1024 * 1024) + 1024;
+    return tc_el_bytes(m) + tc_bs_bytes(n) + 1024;
 }
 
-int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s) {
+size_t tc_el_bytes(int64_t m) {
     using namespace tc;
-    const int m_pad = m_pad_of(t.m);
-    const int n_tiles = n_tiles_of(t.N);
-    const int n_tiles_max = n_tiles_of(t.n);
-    unsigned char* base = (unsigned char*)(((uintptr_t)t.extra + 1023) & ~(uintptr_t)1023);
-    __nv_bfloat16* EL = (__nv_bfloat16*)base;
-    const size_t el_bytes = ((size_t)LIMBS * m_pad * KMAX * 2 + 1023) / 1024 * 1024;
-    __nv_bfloat16* BS = (__nv_bfloat16*)(base + el_bytes);
+    return ((size_t)LIMBS * m_pad_of(m) * KMAX * 2 + 1023) / 1024 * 1024;
+}
+size_t tc_bs_bytes(int64_t n) {
+    using namespace tc;
+    return ((size_t)n_tiles_of(n) * B_ROWS * KMAX * 2 + 1023) / 1024 * 1024;
+}
+int tc_m_pad(int64_t m) { return tc::m_pad_of(m); }
 
+int tc_split_e(const uint32_t* E, int64_t ldE, int b, int64_t m, uint32_t p, const int32_t* k_ptr, void* EL,
+               cudaStream_t s) {
+    using namespace tc;
+    const int m_pad = m_pad_of(m);
+    const int64_t total = (int64_t)m_pad * KMAX;
+    const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
+    split_e_kernel<<<grid, 256, 0, s>>>(E, ldE, b, m, m_pad, p, k_ptr, (__nv_bfloat16*)EL);
+    LNC_CHECK_LAUNCH("split_e_kernel");
+    return LNC_OK;
+}
+
+int tc_gather_split_b(uint32_t* C, int64_t ldc, int64_t N, const int32_t* rows, const int32_t* k_ptr, uint32_t p,
+                      void* BS, bool zero_src, cudaStream_t s) {
+    using namespace tc;
+    gather_split_b_kernel<<<n_tiles_of(N), 256, 0, s>>>(C, ldc, N, rows, k_ptr, p, (__nv_bfloat16*)BS,
+                                                        zero_src ? 1 : 0);
+    LNC_CHECK_LAUNCH("gather_split_b_kernel");
+    return LNC_OK;
+}
+
+int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t N, const int32_t* k_ptr,
+                 bool overwrite, const void* EL, const void* BS, int64_t n_map, int* err, int* status,
+                 cudaStream_t s, bool count_work) {
+    using namespace tc;
+    const int m_pad = m_pad_of(m);
+    const int n_tiles = n_tiles_of(N);
     CUtensorMap mapA, mapB;
-    int rc = make_map(&mapA, EL, KMAX, (uint64_t)LIMBS * m_pad, KC, BM);
+    int rc = make_map(&mapA, const_cast<void*>(EL), KMAX, (uint64_t)LIMBS * m_pad, KC, BM);
     if (rc) return rc;
-    rc = make_map(&mapB, BS, KMAX, (uint64_t)n_tiles_max * B_ROWS, KC, B_ROWS);
+    rc = make_map(&mapB, const_cast<void*>(BS), KMAX, (uint64_t)n_tiles_of(n_map) * B_ROWS, KC, B_ROWS);
     if (rc) return rc;
-
-    const uint32_t p = t.f.p;
-    {
-        const int64_t total = (int64_t)m_pad * KMAX;
-        const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
-        split_e_kernel<<<grid, 256, 0, s>>>(t.E, t.ldE, t.b, t.m, m_pad, p, t.panel_k, EL);
-        LNC_CHECK_LAUNCH("split_e_kernel");
-        gather_split_b_kernel<<<n_tiles, 256, 0, s>>>(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, p, BS);
-        LNC_CHECK_LAUNCH("gather_split_b_kernel");
-    }
+    const uint32_t p = f.p;
     TcParams P;
-    P.C = t.A + t.j1;
-    P.ldc = t.lda;
-    P.m = t.m;
-    P.N = t.N;
+    P.C = C;
+    P.ldc = ldc;
+    P.m = m;
+    P.N = N;
     P.m_pad = m_pad;
     P.n_tiles = n_tiles;
-    P.panel_k = t.panel_k;
-    P.f = t.f;
+    P.panel_k = k_ptr;
+    P.f = f;
     uint64_t w = 1 % p;
     for (int sgrp = 0; sgrp < GROUPS; ++sgrp) {
         P.w[sgrp] = (w > p / 2) ? (int32_t)((int64_t)w - (int64_t)p) : (int32_t)w;
         w = (w * 256) % p;
     }
     P.off = ((((uint64_t)1 << 59) + p - 1) / p) * p;
-    P.err = t.err;
-    P.status = t.status;
+    P.overwrite = overwrite ? 1 : 0;
+    P.err = err;
+    P.status = status;
     LNC_CUDA(cudaFuncSetAttribute(limb_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
     if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }
-    ScopedKernelTimer kt(KC_TRAILING, s);
+    ScopedKernelTimer kt(KC_TRAILING, s, count_work ? (double)m * (double)N * (double)KMAX : 0.0);
     limb_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(mapA, mapB, P);
     LNC_CHECK_LAUNCH("limb_gemm_kernel");
     return LNC_OK;
+}
+
+int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s) {
+    unsigned char* base = (unsigned char*)(((uintptr_t)t.extra + 1023) & ~(uintptr_t)1023);
+    void* EL = base;
+    void* BS = base + tc_el_bytes(t.m);
+    const uint32_t p = t.f.p;
+    int rc = tc_split_e(t.E, t.ldE, t.b, t.m, p, t.panel_k, EL, s);
+    if (rc) return rc;
+    rc = tc_gather_split_b(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, p, BS, true, s);
+    if (rc) return rc;
+    return tc_limb_gemm(t.f, t.A + t.j1, t.lda, t.m, t.N, t.panel_k, false, EL, BS, t.n, t.err, t.status, s,
+                        !t.predicated);
 }
 
 }  // namespace lnc

@@ -186,3 +186,51 @@ def test_strided_input_and_input_not_modified():
     R_ref, _, _ = oracle.rref_modp(np.ascontiguousarray(view), p)
     assert np.array_equal(R.astype(np.uint64), R_ref)
     assert np.array_equal(big, keep)
+
+
+def _extreme_digit_matrix(p, m=384, n=400, seed=0):
+    """First panel = identity on 128 pivot rows; the other rows' panel part and
+    the pivot rows' trailing part are residues whose balanced base-256 digits are
+    (-128, -128, -128, -63), so the limb products summed over the 128-deep
+    contraction exceed 2^22 and the tensor-core epilogue must take its exact
+    float-to-int fallback."""
+    rng = np.random.default_rng(seed)
+    x = -128 * (1 + 256 + 65536) - 63 * 2**24  # centred value with extreme digits
+    xr = x % p
+    A = rng.integers(0, p, size=(m, n), dtype=np.uint64)
+    A[:128, :128] = np.eye(128, dtype=np.uint64)
+    A[:128, 128:] = xr
+    A[128:, :128] = (p - xr) % p
+    return A.astype(np.uint32)
+
+
+@pytest.mark.parametrize("flags", [0, _lib.LNC_FLAG_ROBUST_PANEL])
+def test_limb_gemm_extreme_digits_exact(flags):
+    p = 2**31 - 1
+    A = _extreme_digit_matrix(p)
+    out = np.empty_like(A)
+    piv, rank = rref_host_call(A, p, out, flags=flags)
+    R_ref, piv_ref, _ = oracle.rref_modp(A, p)
+    assert np.array_equal(out.astype(np.uint64), R_ref)
+    assert piv == piv_ref
+
+
+@pytest.mark.parametrize("flags", [0, _lib.LNC_FLAG_ROBUST_PANEL, _lib.LNC_FLAG_SIMT_TRAILING])
+@pytest.mark.parametrize("m,n,r,p", [(900, 700, None, 2**31 - 1), (600, 600, None, 2**31 - 19),
+                                     (1100, 1300, 777, 4294967291)])
+def test_panel_paths_agree_on_adversarial_inputs(flags, m, n, r, p):
+    """Leading rows zero in the leading columns: the candidate-block panel misses
+    pivots there and the exhaustive panel redoes those panels."""
+    rng = np.random.default_rng(m + n)
+    if r is None:
+        A = rng.integers(0, p, size=(m, n), dtype=np.uint64)
+    else:
+        A = workloads.rank_deficient_modp(m, n, r, p, rng)
+    A[: m // 2, :60] = 0
+    A[:, 200:205] = 0
+    A = A.astype(np.uint32)
+    out = np.empty_like(A)
+    piv, rank = rref_host_call(A, p, out, flags=flags)
+    R_ref, piv_ref, _ = oracle.rref_modp(A, p)
+    assert np.array_equal(out.astype(np.uint64), R_ref)
+    assert piv == piv_ref

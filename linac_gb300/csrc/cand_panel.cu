@@ -70,6 +70,56 @@ __device__ __forceinline__ uint32_t cp_inverse(const Mont32& M, uint32_t a) {
     }
 }
 
+// Arithmetic policies of the candidate panel.  `prep` turns a normalised
+// pivot-row value into the form its multiplier uses, `mulp(f, prep(v))` is
+// f * v mod p, `mul` multiplies two ordinary residues.
+struct ArithSmall {  // odd p < 2^31: 32-bit Montgomery, reductions by unsigned min
+    Mont32 M;
+    __device__ ArithSmall(const decltype(CandArgs::M)& c) : M(c) {}
+    __device__ __forceinline__ uint32_t red(uint64_t t) const {
+        const uint32_t lo = (uint32_t)t, hi = (uint32_t)(t >> 32);
+        const uint32_t mh = __umulhi(lo * M.pinv, M.p);
+        const uint32_t u = hi + mh + (lo != 0u ? 1u : 0u);  // < 2p < 2^32
+        return min(u, u - M.p);
+    }
+    __device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b) const { return red((uint64_t)a * b); }
+    __device__ __forceinline__ uint32_t prep(uint32_t v) const { return montmul(v, M.r2); }
+    __device__ __forceinline__ uint32_t mulp(uint32_t f, uint32_t vp) const { return montmul(f, vp); }
+    __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return montmul(montmul(a, b), M.r2); }
+    __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const {
+        const uint32_t d = a - b;
+        return min(d, d + M.p);
+    }
+    __device__ __forceinline__ uint32_t inverse(uint32_t a) const {
+        uint32_t x = montmul(a, M.r2), r = montmul(1u, M.r2);
+        uint32_t e = M.p - 2;
+        while (e) {
+            if (e & 1u) r = montmul(r, x);
+            x = montmul(x, x);
+            e >>= 1;
+        }
+        return red((uint64_t)r);
+    }
+};
+struct ArithMont {  // odd p >= 2^31
+    Mont32 M;
+    __device__ ArithMont(const decltype(CandArgs::M)& c) : M(c) {}
+    __device__ __forceinline__ uint32_t prep(uint32_t v) const { return M.to_mont(v); }
+    __device__ __forceinline__ uint32_t mulp(uint32_t f, uint32_t vp) const { return M.montmul(f, vp); }
+    __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return M.montmul(M.to_mont(a), b); }
+    __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
+    __device__ __forceinline__ uint32_t inverse(uint32_t a) const { return cp_inverse<true>(M, a); }
+};
+struct ArithTwo {  // p = 2
+    Mont32 M;
+    __device__ ArithTwo(const decltype(CandArgs::M)& c) : M(c) {}
+    __device__ __forceinline__ uint32_t prep(uint32_t v) const { return v; }
+    __device__ __forceinline__ uint32_t mulp(uint32_t f, uint32_t vp) const { return M.barrett((uint64_t)f * vp); }
+    __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return M.barrett((uint64_t)a * b); }
+    __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
+    __device__ __forceinline__ uint32_t inverse(uint32_t) const { return 1u; }
+};
+
 // block-wide exclusive scan of a 0/1 flag (blockDim.x <= 1024); returns the
 // prefix, writes the total to *total (shared)
 __device__ __forceinline__ int block_scan_flag(int flag, int* s_warp, int* total) {
@@ -94,20 +144,24 @@ __device__ __forceinline__ int block_scan_flag(int flag, int* s_warp, int* total
     return r;
 }
 
-template <bool MONT>
+template <class Arith>
 __global__ void __launch_bounds__(kCandThreads, 1) cand_panel_kernel(CandArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int bw = a.bw;
-    uint32_t* tile = (uint32_t*)smem_raw;                 // [smax][bw]
-    uint32_t* nprM = tile + (size_t)a.smax * bw;          // [kMaxPanel]
+    // column-major block, odd pitch: a column (fixed c, consecutive rows) and a
+    // row (fixed i, consecutive columns) are both free of bank conflicts
+    const int LDT = a.smax | 1;
+    uint32_t* tile = (uint32_t*)smem_raw;                 // [bw][LDT]
+    uint32_t* nprM = tile + (size_t)LDT * kMaxPanel;      // [kMaxPanel]
     uint32_t* fcol = nprM + kMaxPanel;                    // [256]
     __shared__ int s_cand[256];
     __shared__ uint8_t s_isp[256];
     __shared__ int s_pr[kMaxPanel], s_pc[kMaxPanel];
     __shared__ int s_warp[32];
-    __shared__ int s_n, s_total, s_next, s_min;
-    __shared__ uint32_t s_inv;
-    const Mont32 M = a.M;
+    __shared__ int s_n, s_total, s_next;
+    __shared__ int s_npi;           // look-ahead: pivot row of the next column (-1: none)
+    __shared__ uint32_t s_ninv;     // and the inverse of its entry
+    const Arith ar(a.M);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     constexpr int NW = kCandThreads / 32;
 
@@ -151,49 +205,97 @@ __global__ void __launch_bounds__(kCandThreads, 1) cand_panel_kernel(CandArgs a)
     // ---- load the candidate block
     for (int i = warp; i < n; i += NW) {
         const uint32_t* src = a.A + (int64_t)s_cand[i] * a.lda + a.j0;
-        for (int c = lane; c < bw; c += 32) tile[(size_t)i * bw + c] = src[c];
+        for (int c = lane; c < bw; c += 32) tile[(size_t)c * LDT + i] = src[c];
     }
     for (int i = tid; i < 256; i += blockDim.x) s_isp[i] = 0;
     __syncthreads();
 
-    // ---- Gauss-Jordan on the block, transform kept in the pivot columns
+    // ---- Gauss-Jordan on the block, transform kept in the pivot columns.
+    // Look-ahead: while warps 1.. eliminate column c's pivot from the rest of the
+    // block, warp 0 first brings column c+1 up to date, picks its pivot row and
+    // computes the inverse, so the serial inverse overlaps the bulk update.
+    // Lanes run over rows, so each lane keeps its rows' multipliers in registers.
+    constexpr int RPL = (kCandRows + 31) / 32;  // rows per lane (n <= kCandRows)
+    auto pick_pivot = [&](int col, int exclude) {
+        // warp 0: first candidate row, not a pivot row and not `exclude`, with a
+        // non-zero entry in column `col`; lane 0 then computes its inverse
+        int found = -1;
+        const uint32_t* colp = tile + (size_t)col * LDT;
+        for (int base = 0; base < n && found < 0; base += 32) {
+            const int i = base + lane;
+            const bool ok = i < n && !s_isp[i] && i != exclude && colp[i] != 0u;
+            const unsigned b = __ballot_sync(0xffffffffu, ok);
+            if (b) found = base + __ffs(b) - 1;
+        }
+        if (lane == 0) {
+            s_npi = found;
+            s_ninv = (found >= 0) ? ar.inverse(colp[found]) : 0u;
+        }
+    };
+    if (warp == 0) pick_pivot(0, -1);
+    __syncthreads();
     int k = 0;
     for (int c = 0; c < bw; ++c) {
-        if (tid == 0) s_min = 0x7fffffff;
-        __syncthreads();
-        if (tid < n && !s_isp[tid] && tile[(size_t)tid * bw + c] != 0u) atomicMin(&s_min, tid);
-        __syncthreads();
-        const int pi = s_min;
-        if (pi == 0x7fffffff) continue;  // no pivot in this column among the candidates
-        if (tid < n) fcol[tid] = tile[(size_t)tid * bw + c];
-        if (tid == 0) s_inv = cp_inverse<MONT>(M, tile[(size_t)pi * bw + c]);
-        __syncthreads();
-        const uint32_t inv = s_inv;
+        const int pi = s_npi;
+        const uint32_t inv = s_ninv;
+        if (pi < 0) {
+            // column c has no pivot: nothing changes, look at column c + 1
+            __syncthreads();
+            if (warp == 0 && c + 1 < bw) pick_pivot(c + 1, -1);
+            __syncthreads();
+            continue;
+        }
+        // normalised pivot row (its column c holds the inverse: the transform) and
+        // the multipliers of every other row
         for (int cc = tid; cc < bw; cc += blockDim.x) {
-            uint32_t v;
-            if constexpr (MONT) {
-                v = (cc == c) ? inv : M.montmul(M.to_mont(tile[(size_t)pi * bw + cc]), inv);
-                nprM[cc] = M.to_mont(v);
-            } else {
-                v = (cc == c) ? inv : M.barrett((uint64_t)tile[(size_t)pi * bw + cc] * inv);
-                nprM[cc] = v;
+            uint32_t* e = tile + (size_t)cc * LDT + pi;
+            const uint32_t v = (cc == c) ? inv : ar.mul(*e, inv);
+            nprM[cc] = ar.prep(v);
+            *e = v;
+        }
+        for (int i = tid; i < n; i += blockDim.x) fcol[i] = (i == pi) ? 0u : tile[(size_t)c * LDT + i];
+        __syncthreads();
+        // this lane's rows and their multipliers (0 for the pivot row and absent rows)
+        uint32_t fr[RPL];
+#pragma unroll
+        for (int j = 0; j < RPL; ++j) {
+            const int i = lane + 32 * j;
+            fr[j] = (i < n) ? fcol[i] : 0u;
+        }
+        if (warp == 0) {
+            if (c + 1 < bw) {
+                uint32_t* colp = tile + (size_t)(c + 1) * LDT;
+                const uint32_t vp = nprM[c + 1];
+#pragma unroll
+                for (int j = 0; j < RPL; ++j) {
+                    const int i = lane + 32 * j;
+                    if (fr[j] != 0u) colp[i] = ar.sub(colp[i], ar.mulp(fr[j], vp));
+                }
+                __syncwarp();
+                pick_pivot(c + 1, pi);
             }
-            tile[(size_t)pi * bw + cc] = v;
+        } else {
+            // target columns: right of c + 1, then the transform columns (earlier
+            // pivot columns and c).  Earlier columns without a pivot are zero in the
+            // pivot row and stay as they are.
+            const int nright = bw - c - 2 > 0 ? bw - c - 2 : 0;
+            const int ntarget = nright + k + 1;
+            for (int t = warp - 1; t < ntarget; t += NW - 1) {
+                const int cc = (t < nright) ? c + 2 + t : ((t - nright < k) ? s_pc[t - nright] : c);
+                uint32_t* colp = tile + (size_t)cc * LDT;
+                const uint32_t vp = nprM[cc];
+                const bool zero_first = (cc == c);
+#pragma unroll
+                for (int j = 0; j < RPL; ++j) {
+                    const int i = lane + 32 * j;
+                    if (fr[j] != 0u) {
+                        const uint32_t x = zero_first ? 0u : colp[i];
+                        colp[i] = ar.sub(x, ar.mulp(fr[j], vp));
+                    }
+                }
+            }
         }
         __syncthreads();
-        for (int i = warp; i < n; i += NW) {
-            if (i == pi) continue;
-            const uint32_t f = fcol[i];
-            if (f == 0u) continue;
-            uint32_t* row = tile + (size_t)i * bw;
-            for (int cc = lane; cc < bw; cc += 32) {
-                const uint32_t x = (cc == c) ? 0u : row[cc];
-                uint32_t prod;
-                if constexpr (MONT) prod = M.montmul(f, nprM[cc]);
-                else prod = M.barrett((uint64_t)f * nprM[cc]);
-                row[cc] = M.sub(x, prod);
-            }
-        }
         if (tid == 0) {
             s_pr[k] = pi;
             s_pc[k] = c;
@@ -207,7 +309,7 @@ __global__ void __launch_bounds__(kCandThreads, 1) cand_panel_kernel(CandArgs a)
     const int64_t rank0 = *a.rank;
     for (int idx = tid; idx < kMaxPanel * kMaxPanel; idx += blockDim.x) {
         const int t = idx / kMaxPanel, u = idx % kMaxPanel;
-        a.X[idx] = (t < k && u < k) ? tile[(size_t)s_pr[t] * bw + s_pc[u]] : 0u;
+        a.X[idx] = (t < k && u < k) ? tile[(size_t)s_pc[u] * LDT + s_pr[t]] : 0u;
     }
     for (int t = tid; t < k; t += blockDim.x) {
         const int r = s_cand[s_pr[t]];
@@ -298,21 +400,20 @@ __global__ void check_missed_kernel(const uint32_t* A, int64_t lda, int64_t m, i
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(missed, 1);
 }
 
-int launch_cand_panel(const CandArgs& a, cudaStream_t s) {
-    const size_t smem = (size_t)a.smax * a.bw * 4 + kMaxPanel * 4 + 256 * 4;
-    void* args[] = {(void*)&a};
-    if (a.M.p & 1u) {
-        LNC_CUDA(cudaFuncSetAttribute(cand_panel_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        ScopedKernelTimer kt(KC_PANEL, s, 2.0 * a.smax * a.bw * 4.0);
-        cand_panel_kernel<true><<<1, kCandThreads, smem, s>>>(a);
-    } else {
-        LNC_CUDA(cudaFuncSetAttribute(cand_panel_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        ScopedKernelTimer kt(KC_PANEL, s, 2.0 * a.smax * a.bw * 4.0);
-        cand_panel_kernel<false><<<1, kCandThreads, smem, s>>>(a);
-    }
-    (void)args;
+template <class Arith>
+static int launch_cand_typed(const CandArgs& a, size_t smem, cudaStream_t s) {
+    LNC_CUDA(cudaFuncSetAttribute(cand_panel_kernel<Arith>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ScopedKernelTimer kt(KC_PANEL, s, 2.0 * a.smax * a.bw * 4.0);
+    cand_panel_kernel<Arith><<<1, kCandThreads, smem, s>>>(a);
     LNC_CHECK_LAUNCH("cand_panel_kernel");
     return LNC_OK;
+}
+
+int launch_cand_panel(const CandArgs& a, cudaStream_t s) {
+    const size_t smem = (size_t)(a.smax | 1) * kMaxPanel * 4 + kMaxPanel * 4 + 256 * 4;
+    if (!(a.M.p & 1u)) return launch_cand_typed<ArithTwo>(a, smem, s);
+    if (a.M.p < (1u << 31)) return launch_cand_typed<ArithSmall>(a, smem, s);
+    return launch_cand_typed<ArithMont>(a, smem, s);
 }
 
 int launch_split_g(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, uint32_t p, const int32_t* panel_k,

@@ -75,6 +75,7 @@ struct TcParams {
     int32_t w[GROUPS];      // 256^s mod p, centred
     uint64_t off;           // multiple of p >= 2^59 (makes the 64-bit sum non-negative)
     int overwrite;          // 1: C <- E * B (C is not read), 0: C <- C + E * B
+    uint32_t pinv;          // -p^-1 mod 2^32 (Montgomery reduction of the epilogue sum)
     int* err;
     int* status;
 };
@@ -149,6 +150,22 @@ __device__ __forceinline__ void flag_error(const TcParams& P, volatile int* cta_
     atomicExch(P.status, LNC_ERR_TIMEOUT);
 }
 
+// v mod p for the epilogue sum v < 2^60: Montgomery (v 2^-32; the weights
+// already carry the factor 2^32) when 2^30 <= p < 2^31, else Barrett.
+template <bool REDC>
+__device__ __forceinline__ uint32_t reduce_sum(const FieldU32& f, uint32_t pinv, uint64_t v) {
+    if constexpr (REDC) {
+        const uint32_t lo = (uint32_t)v;
+        const uint32_t u = (uint32_t)(v >> 32) + __umulhi(lo * pinv, f.p) + (lo != 0u ? 1u : 0u);  // < 2p
+        return min(u, u - f.p);
+    } else {
+        return f.reduce64(v);
+    }
+}
+
+// REDC: 2^30 <= p < 2^31, the weights carry an extra factor 2^32 and the
+// 64-bit sum is reduced by one Montgomery step; otherwise Barrett.
+template <bool REDC>
 __global__ void __launch_bounds__(THREADS, 1)
     limb_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const TcParams P) {
@@ -324,15 +341,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&acc_empty[buf]);
-            // exact conversion: for |x| < 2^22, x + 1.5 * 2^23 is exact and its bit pattern minus
-            // 0x4B400000 is x (full-rate FADD instead of the quarter-rate F2I); the weighted sum is
-            // formed modulo 2^64, its true value off + sum x_g w_g lies in [0, 2^60]
+            // exact conversion: for |x| <= 2^22, x + 1.5 * 2^23 is exact and its bit pattern minus
+            // 0x4B400000 is x (full-rate FADD instead of the quarter-rate F2I).  Groups 0, 1, 5, 6 hold
+            // at most two digit products per step and stay within 2^22 for any input; groups 2-4 are
+            // checked.  The weighted sum is formed modulo 2^64; its true value lies in [0, 2^60].
             float mx = 0.f;
 #pragma unroll
-            for (int g = 0; g < GROUPS; ++g)
+            for (int g = 2; g <= 4; ++g)
 #pragma unroll
                 for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
-            const bool fast = mx < 4194304.0f;
+            const bool fast = mx <= 4194304.0f;
             uint32_t res[16];
             if (__all_sync(0xffffffffu, fast)) {
 #pragma unroll
@@ -343,7 +361,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         const int32_t y = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F));
                         v += (uint64_t)((int64_t)y * (int64_t)P.w[g]);
                     }
-                    res[c] = f.add(old[c], f.reduce64(v));
+                    res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
                 }
             } else {
 #pragma unroll
@@ -352,7 +370,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                     for (int g = 0; g < GROUPS; ++g)
                         v += (uint64_t)((int64_t)__float2int_rn(__uint_as_float(d[g][c])) * (int64_t)P.w[g]);
-                    res[c] = f.add(old[c], f.reduce64(v));
+                    res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
                 }
             }
             if (vec) {
@@ -492,20 +510,27 @@ int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t
     P.n_tiles = n_tiles;
     P.panel_k = k_ptr;
     P.f = f;
-    uint64_t w = 1 % p;
+    const bool redc = (p & 1u) && p >= (1u << 30) && p < (1u << 31);
+    uint64_t w = redc ? (((uint64_t)1 << 32) % p) : (1 % p);  // 2^32 folded in for the Montgomery step
     for (int sgrp = 0; sgrp < GROUPS; ++sgrp) {
         P.w[sgrp] = (w > p / 2) ? (int32_t)((int64_t)w - (int64_t)p) : (int32_t)w;
         w = (w * 256) % p;
     }
     P.off = ((((uint64_t)1 << 59) + p - 1) / p) * p;
     P.overwrite = overwrite ? 1 : 0;
+    {
+        uint32_t x = p;
+        for (int i = 0; i < 5; ++i) x *= 2u - p * x;
+        P.pinv = 0u - x;
+    }
     P.err = err;
     P.status = status;
-    LNC_CUDA(cudaFuncSetAttribute(limb_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+    auto kern = redc ? limb_gemm_kernel<true> : limb_gemm_kernel<false>;
+    LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
     if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }
     ScopedKernelTimer kt(KC_TRAILING, s, count_work ? (double)m * (double)N * (double)KMAX : 0.0);
-    limb_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(mapA, mapB, P);
+    kern<<<grid, THREADS, SMEM_BYTES, s>>>(mapA, mapB, P);
     LNC_CHECK_LAUNCH("limb_gemm_kernel");
     return LNC_OK;
 }

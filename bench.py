@@ -51,6 +51,10 @@ WORKLOADS = {
     "rref_u32_20000": dict(m=20000, n=20000, p=P31, dtype="u32"),
     "rref_u32_8192": dict(m=8192, n=8192, p=P31, dtype="u32"),
     "rref_u32_4096": dict(m=4096, n=4096, p=P31, dtype="u32"),
+    # uneven batch: m ~ U[64, 2048], n = round(m U[0.8, 1.25]), rank deficit ~ U[0, 10%],
+    # a prime per matrix from the 64 largest primes below 2^31, built as B.C on the device
+    "batch4096": dict(count=4096, m_lo=64, m_hi=2048, dtype="u32", batch=True),
+    "batch512": dict(count=512, m_lo=64, m_hi=2048, dtype="u32", batch=True),
 }
 
 
@@ -442,6 +446,146 @@ def run_reference(args, dist: Dist):
     }
 
 
+def build_batch_on_device(plan, specs, seed: int):
+    """Write every matrix of the batch into the plan's input buffer on the
+    device: uniform residues for full-rank matrices, B.C for deficient ones."""
+    from linac_gb300 import _lib
+    L = _lib.lib()
+    s = plan.stream.handle
+    big = max(max(m * r, r * n) for m, n, r, p in specs)
+    dB = _lib.DeviceBuffer(4 * big)
+    dC = _lib.DeviceBuffer(4 * big)
+    for i, ((m, n, r, p), off) in enumerate(zip(specs, plan.offsets)):
+        dst = plan.d_in.ptr + off
+        if r >= min(m, n):
+            _lib.check(L.lnc_fill_uniform_modp(dst, m * n, p, seed * 100003 + i, _lib.LNC_U32, s))
+        else:
+            _lib.check(L.lnc_fill_uniform_modp(dB.ptr, m * r, p, seed * 100003 + 2 * i + 1, _lib.LNC_U32, s))
+            _lib.check(L.lnc_fill_uniform_modp(dC.ptr, r * n, p, seed * 100003 + 2 * i + 2, _lib.LNC_U32, s))
+            _lib.check(L.lnc_matmul_modp_device(_lib.LNC_U32, m, r, n, p, dB.ptr, r, dC.ptr, n, dst, n, s))
+    plan.stream.synchronize()
+    dB.close()
+    dC.close()
+
+
+def run_batch(args, dist: Dist):
+    """Batched RREF of the uneven batch (one CUDA-graph launch per run) against
+    the plain path: one cuda_row_reduce call per matrix on the same inputs."""
+    from linac_gb300 import _lib, cuda_row_reduce, pinned_empty
+    from linac_gb300 import workloads
+    from linac_gb300.batch import BatchPlan, autotune
+    import oracle
+
+    if dist.world > 1:
+        _lib.check(_lib.lib().lnc_set_device(dist.local_rank))
+    wl = WORKLOADS[args.workload]
+    rng = np.random.default_rng(2024 + dist.rank)
+    specs = workloads.batch_shapes(wl["count"], rng, wl["m_lo"], wl["m_hi"])
+    shapes = [(m, n) for m, n, r, p in specs]
+    primes = [p for m, n, r, p in specs]
+    t_tune = time.perf_counter()
+    tpc, cand = (0, 0) if args.no_tune else autotune(shapes, primes)
+    t_tune = time.perf_counter() - t_tune
+    plan = BatchPlan(shapes, primes, tpc, cand)
+    build_batch_on_device(plan, specs, seed=7 + dist.rank)
+    for _ in range(args.warmup):
+        plan.run()
+    redone = plan.finish()
+    _lib.kernel_timing(True)
+    ev = [(_lib.Event(), _lib.Event()) for _ in range(args.steps)]
+    dist.barrier()
+    _lib.check(_lib.lib().lnc_device_synchronize())
+    launches0 = _lib.launch_count()
+    with ClockSampler(dist.local_rank if dist.world > 1 else 0) as clk:
+        for i in range(args.steps):
+            ev[i][0].record(plan.stream.handle)
+            plan.run()
+            ev[i][1].record(plan.stream.handle)
+        plan.stream.synchronize()
+    launches = _lib.launch_count() - launches0
+    lat = [a.elapsed_ms(b) for a, b in ev]
+    _lib.kernel_timing(False)
+    redone = plan.finish()
+    total_s = dist.max(sum(lat) / 1000.0)
+    solves = dist.sum(float(args.steps * len(specs)))
+    value = solves / total_s
+    # ---- correctness: rank and pivots of every matrix; full oracle check on a sample
+    pivs, ranks = plan.pivots_and_ranks()
+    expect = [min(r, m, n) for m, n, r, p in specs]
+    ok = all(int(rk) == e and list(pv) == list(range(e)) for rk, e, pv in zip(ranks, expect, pivs))
+    packed_in = pinned_empty((plan.total_bytes,), np.uint8)
+    _lib.check(_lib.lib().lnc_memcpy_d2h(packed_in.ctypes.data, plan.d_in.ptr, plan.total_bytes, plan.stream.handle))
+    packed_out = pinned_empty((plan.total_bytes,), np.uint8)
+    plan.download_packed(packed_out)
+    ins, outs = plan.unpack(packed_in), plan.unpack(packed_out)
+    small = [i for i in np.argsort([m * n for m, n in shapes])[:6]]
+    for i in small:
+        R_ref, _, _ = oracle.rref_modp(ins[i], primes[i])
+        ok = ok and bool(np.array_equal(outs[i].astype(np.uint64), R_ref))
+    # ---- end-to-end batched: pack (pinned) -> H2D -> graph -> D2H
+    t0 = time.perf_counter()
+    plan.upload_packed(packed_in)
+    plan.run()
+    plan.finish()
+    plan.download_packed(packed_out)
+    t_e2e = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.sum(float(len(specs))) / t_e2e
+    # ---- plain path: one cuda_row_reduce call per matrix (host arrays), on a sample
+    sample = rng.choice(len(specs), size=min(args.plain_sample, len(specs)), replace=False)
+    cuda_row_reduce(ins[sample[0]], primes[sample[0]])
+    t0 = time.perf_counter()
+    for i in sample:
+        cuda_row_reduce(ins[i], primes[i])
+    t_plain = time.perf_counter() - t0
+    plain_value = len(sample) / t_plain * (sum(m * n * min(m, n) for m, n in shapes) / len(shapes)) / \
+        (sum(shapes[i][0] * shapes[i][1] * min(shapes[i]) for i in sample) / len(sample))
+    work = sum(float(m) * sum(n - c for c in range(min(r, m, n))) for m, n, r, p in specs)
+    kb = _lib.kernel_timing_read(_lib.KC_BATCH)
+    peaks = measured_peaks()
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": sum(lat) / len(lat),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32",
+        "data": "synthetic (device SplitMix64 residues; deficient matrices as B.C mod p)",
+        "config": {"workload": f"batch of {len(specs)} uneven matrices, m ~ U[{wl['m_lo']},{wl['m_hi']}], "
+                               "n = round(m U[0.8,1.25]), rank deficit U[0,10%], 64 primes < 2^31",
+                   "count": len(specs), "tiles_per_cta": tpc, "cand_rows": cand,
+                   "autotune_s": t_tune, "graph": "one CUDA-graph launch per batch",
+                   "l2": f"batch inputs {plan.total_bytes / 1e9:.1f} GB > L2"},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "note": "makespan of one whole-batch launch"},
+        "bit_exact": bool(ok),
+        "redone_exhaustively": int(redone),
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": plan.total_bytes,
+                "d2h_bytes_per_step": plan.total_bytes, "call": "linac_gb300.batch.BatchPlan (pack, run, unpack)"},
+        "plain": {"value": plain_value, "unit": "solves/s", "sample": int(len(sample)),
+                  "call": "linac_gb300.cuda_row_reduce per matrix (host arrays)",
+                  "note": "sample rate scaled to the batch's mean m*n*min(m,n)"},
+        "batched_vs_plain": value / plain_value,
+        "batched_e2e_vs_plain": e2e_value / plain_value,
+        "gpu_launches": launches,
+        "work_field_macs_per_batch": work,
+        "device_bytes": plan.device_bytes,
+        "roofline": {"bound": "tensor", "kernel": "batched limb GEMM + candidate panels (whole graph)",
+                     "achieved": 32.0 * work / (sum(lat) / len(lat) / 1e3) / 1e12,
+                     "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                     "frac": 32.0 * work / (sum(lat) / len(lat) / 1e3) / 1e12 / peaks["bf16_tflops_sustained"],
+                     "traffic": None, "peak_source": f"{peaks['source']} bf16 sustained",
+                     "note": "whole-graph time incl. panels and splits; 2*4*4 bf16 flops per field multiply-add"},
+        "clocks": clk.summary(),
+    }
+    plan.close()
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -455,6 +599,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--ref-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="batched workloads: skip the autotuner")
+    ap.add_argument("--plain-sample", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     dist = Dist()
@@ -466,7 +612,10 @@ def main():
         from linac_gb300 import _lib  # fails loudly if the library is missing
         args.flags = (_lib.LNC_FLAG_SIMT_TRAILING if args.simt else 0) | \
             (_lib.LNC_FLAG_ROBUST_PANEL if args.robust_panel else 0)
-        line = run_ours(args, dist)
+        if WORKLOADS[args.workload].get("batch"):
+            line = run_batch(args, dist)
+        else:
+            line = run_ours(args, dist)
     if dist.rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
     dist.close()

@@ -140,6 +140,49 @@ int lnc_rref_device_noalloc(int dtype, int64_t m, int64_t n, uint64_t p, double 
                             int64_t ld_work, void* dev_out, int64_t ld_out, int64_t* dev_pivot_cols,
                             int64_t* dev_rank, void* stream, int flags);
 
+/* ---- batched RREF (many uneven matrices, a prime each) ---------------------- */
+typedef struct lnc_batch_matrix {
+    uint64_t p;             /* prime, < 2^32 */
+    int64_t m, n;
+    const void* dev_in;     /* m x n input (not modified), leading dimension ld_in */
+    int64_t ld_in;
+    void* dev_out;          /* m x n RREF, leading dimension ld_out */
+    int64_t ld_out;
+    int64_t* dev_pivot_cols; /* optional: min(m,n) pivot columns, -1 past the rank */
+    int64_t* dev_rank;       /* optional */
+} lnc_batch_matrix;
+
+/*
+ * Plan a batched RREF of `count` matrices (LNC_U32 only): allocates one
+ * scratch arena, records every launch of every panel step and captures them
+ * into one CUDA graph.  tiles_per_cta / cand_rows tune the contraction work
+ * split and the candidate-block height (0 = defaults).  The plan can be run
+ * any number of times on new contents of the same buffers.
+ * No counterpart in the reference: linac reduces one matrix per
+ * cuda_row_reduce call (linac/pycuda_row_reduce.py:18-151); its callers loop
+ * (linac/vector_spaces/over_function_fields.py:74-101).
+ */
+int lnc_batch_plan_create(int dtype, const lnc_batch_matrix* mats, int64_t count, int tiles_per_cta,
+                          int cand_rows, void* stream, void** plan);
+/* One graph launch on `stream` (asynchronous). */
+int lnc_batch_plan_run(void* plan, void* stream);
+/* Synchronise; redo any matrix whose candidate panels missed a pivot with the
+ * exhaustive path; *n_redo (optional) receives how many. */
+int lnc_batch_plan_finish(void* plan, void* stream, int64_t* n_redo);
+/* Device bytes held by the plan (admission accounting). */
+int64_t lnc_batch_plan_bytes(void* plan);
+int lnc_batch_plan_destroy(void* plan);
+/* create + run + finish + destroy */
+int lnc_rref_batch_device(int dtype, const lnc_batch_matrix* mats, int64_t count, void* stream, int flags);
+
+/* ---- workload helpers (no counterpart in the reference) --------------------- */
+/* Fill `count` residues uniform in [0, p) from `seed` (LNC_U32 / LNC_U64). */
+int lnc_fill_uniform_modp(void* dev_ptr, int64_t count, uint64_t p, uint64_t seed, int dtype, void* stream);
+/* C = A B mod p, A m x k, B k x n, exact (LNC_U32, tensor-core limb GEMM);
+ * used to build rank-deficient inputs B.C on the device. */
+int lnc_matmul_modp_device(int dtype, int64_t m, int64_t k, int64_t n, uint64_t p, const void* A, int64_t lda,
+                           const void* B, int64_t ldb, void* C, int64_t ldc, void* stream);
+
 /* ---- monomial loader --------------------------------------------------------- */
 /*
  * out[r, c] = prod_{t<degree} bases[r, lindices[c, t]] (mod p for LNC_U32 /

@@ -95,6 +95,8 @@ _SIGNATURES = {
     "lnc_rref_device": ([_int, _i64, _i64, _u64, _dbl, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _int], _int),
     "lnc_load_matrix_host": ([_int, _i64, _i64, _i64, _i64, _u64, _vp, _vp, _vp], _int),
     "lnc_load_matrix_device": ([_int, _i64, _i64, _i64, _i64, _u64, _vp, _vp, _vp, _i64, _vp], _int),
+    "lnc_fill_uniform_modp": ([_vp, _i64, _u64, _u64, _int, _vp], _int),
+    "lnc_matmul_modp_device": ([_int, _i64, _i64, _i64, _u64, _vp, _i64, _vp, _i64, _vp, _i64, _vp], _int),
 }
 
 

@@ -1,0 +1,262 @@
+"""Batched RREF of many uneven matrices over F_p (a prime per matrix).
+
+linac reduces one matrix per ``cuda_row_reduce`` call and its callers loop
+(linac/vector_spaces/over_function_fields.py:74-101,
+linac/linear_system_solver.py:41-45).  ``rref_batch`` reduces a whole list in
+one CUDA-graph launch of the tensor-core path (csrc/batch.cu); ``BatchPlan``
+keeps the device buffers and the captured graph so that a batch of the same
+shapes can be re-run on new contents without re-planning.
+
+The work split of the contraction kernels (output tiles per CTA) and the
+candidate-block height are chosen by ``autotune`` from timings on a sample of
+the batch, cached per size signature in ``$LINAC_GB300_CACHE`` (default
+``~/.cache/linac_gb300/autotune.json``).
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import time
+
+import numpy as np
+
+from . import _lib
+from .primes import check_prime
+
+
+class lnc_batch_matrix(ctypes.Structure):
+    _fields_ = [("p", ctypes.c_uint64), ("m", ctypes.c_int64), ("n", ctypes.c_int64),
+                ("dev_in", ctypes.c_void_p), ("ld_in", ctypes.c_int64),
+                ("dev_out", ctypes.c_void_p), ("ld_out", ctypes.c_int64),
+                ("dev_pivot_cols", ctypes.c_void_p), ("dev_rank", ctypes.c_void_p)]
+
+
+_bound = False
+
+
+def _bind():
+    global _bound
+    if _bound:
+        return
+    vp, i64, ci = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    _lib.bind("lnc_batch_plan_create", [ci, vp, i64, ci, ci, vp, vp])
+    _lib.bind("lnc_batch_plan_run", [vp, vp])
+    _lib.bind("lnc_batch_plan_finish", [vp, vp, vp])
+    _lib.bind("lnc_batch_plan_bytes", [vp], i64)
+    _lib.bind("lnc_batch_plan_destroy", [vp])
+    _lib.bind("lnc_rref_batch_device", [ci, vp, i64, vp, ci])
+    _bound = True
+
+
+def _align(x: int, a: int = 256) -> int:
+    return (x + a - 1) // a * a
+
+
+class BatchPlan:
+    """Device buffers + captured graph for one list of matrix shapes."""
+
+    def __init__(self, shapes, primes, tiles_per_cta: int = 0, cand_rows: int = 0, stream=None):
+        _bind()
+        self.shapes = [(int(m), int(n)) for m, n in shapes]
+        self.primes = [int(p) for p in primes]
+        if len(self.shapes) != len(self.primes) or not self.shapes:
+            raise ValueError("need one prime per matrix and at least one matrix")
+        for p in set(self.primes):
+            if p >= 2**32:
+                raise ValueError("the batched path serves primes below 2^32")
+            check_prime(p)
+        self.stream = stream if stream is not None else _lib.Stream()
+        s = self.stream.handle
+        self.offsets = []
+        off = 0
+        for m, n in self.shapes:
+            self.offsets.append(off)
+            off += _align(4 * m * n)
+        self.total_bytes = off
+        self.d_in = _lib.DeviceBuffer(off)
+        self.d_out = _lib.DeviceBuffer(off)
+        kmax = [min(m, n) for m, n in self.shapes]
+        self.piv_off = np.concatenate([[0], np.cumsum(kmax)]).astype(np.int64)
+        self.d_piv = _lib.DeviceBuffer(8 * int(self.piv_off[-1]) + 8)
+        self.d_rank = _lib.DeviceBuffer(8 * len(self.shapes))
+        descs = (lnc_batch_matrix * len(self.shapes))()
+        for i, ((m, n), p) in enumerate(zip(self.shapes, self.primes)):
+            d = descs[i]
+            d.p, d.m, d.n = p, m, n
+            d.dev_in = self.d_in.ptr + self.offsets[i]
+            d.ld_in = n
+            d.dev_out = self.d_out.ptr + self.offsets[i]
+            d.ld_out = n
+            d.dev_pivot_cols = self.d_piv.ptr + 8 * int(self.piv_off[i])
+            d.dev_rank = self.d_rank.ptr + 8 * i
+        self._descs = descs
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().lnc_batch_plan_create(_lib.LNC_U32, ctypes.addressof(descs), len(self.shapes),
+                                                    int(tiles_per_cta), int(cand_rows), s, ctypes.byref(h)),
+                   "lnc_batch_plan_create")
+        self.handle = h.value
+        self.redone = 0
+
+    @property
+    def device_bytes(self) -> int:
+        return int(_lib.lib().lnc_batch_plan_bytes(self.handle)) + 2 * self.total_bytes
+
+    def upload_packed(self, host_packed: np.ndarray):
+        """Copy a packed host buffer (layout of ``pack``) to the device input."""
+        _lib.check(_lib.lib().lnc_memcpy_h2d(self.d_in.ptr, host_packed.ctypes.data, self.total_bytes,
+                                             self.stream.handle))
+
+    def pack(self, matrices, out: np.ndarray | None = None) -> np.ndarray:
+        """Pack matrices into one host buffer (uint8 view of the device layout)."""
+        buf = out if out is not None else np.empty(self.total_bytes, dtype=np.uint8)
+        for (m, n), off, A in zip(self.shapes, self.offsets, matrices):
+            view = buf[off:off + 4 * m * n].view(np.uint32).reshape(m, n)
+            np.copyto(view, A, casting="unsafe")
+        return buf
+
+    def run(self):
+        _lib.check(_lib.lib().lnc_batch_plan_run(self.handle, self.stream.handle), "lnc_batch_plan_run")
+
+    def finish(self) -> int:
+        n = ctypes.c_int64(0)
+        _lib.check(_lib.lib().lnc_batch_plan_finish(self.handle, self.stream.handle, ctypes.byref(n)),
+                   "lnc_batch_plan_finish")
+        self.redone = int(n.value)
+        return self.redone
+
+    def download_packed(self, host_packed: np.ndarray):
+        _lib.check(_lib.lib().lnc_memcpy_d2h(host_packed.ctypes.data, self.d_out.ptr, self.total_bytes,
+                                             self.stream.handle))
+        self.stream.synchronize()
+        return host_packed
+
+    def unpack(self, host_packed: np.ndarray):
+        return [host_packed[off:off + 4 * m * n].view(np.uint32).reshape(m, n)
+                for (m, n), off in zip(self.shapes, self.offsets)]
+
+    def pivots_and_ranks(self):
+        piv = np.empty(int(self.piv_off[-1]) + 1, dtype=np.int64)
+        self.d_piv.download(piv, self.stream.handle)
+        ranks = np.empty(len(self.shapes), dtype=np.int64)
+        self.d_rank.download(ranks, self.stream.handle)
+        return [list(piv[self.piv_off[i]:self.piv_off[i] + ranks[i]]) for i in range(len(self.shapes))], ranks
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.lib().lnc_batch_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True):
+    """RREF of every matrix of the list over F_{primes[i]} (uint32 residues).
+
+    Returns the list of RREFs (uint32 arrays), and the pivot columns when
+    ``return_pivots``.  One plan (one CUDA graph) covers the whole list.
+    """
+    mats = [np.asarray(A) for A in matrices]
+    if isinstance(primes, (int, np.integer)):
+        primes = [int(primes)] * len(mats)
+    shapes = [A.shape for A in mats]
+    tpc, cand = autotune(shapes, primes) if tune else (0, 0)
+    plan = BatchPlan(shapes, primes, tpc, cand)
+    try:
+        host = plan.pack(mats)
+        plan.upload_packed(host)
+        plan.run()
+        plan.finish()
+        out = plan.download_packed(np.empty(plan.total_bytes, dtype=np.uint8))
+        res = [R.copy() for R in plan.unpack(out)]
+        if return_pivots:
+            pivs, _ = plan.pivots_and_ranks()
+            return res, [[int(x) for x in p] for p in pivs]
+        return res
+    finally:
+        plan.close()
+
+
+# ---------------------------------------------------------------------------
+# autotuner
+# ---------------------------------------------------------------------------
+TILE_CHOICES = (4, 8, 16, 32)
+CAND_CHOICES = (136, 160)
+
+
+def _cache_path() -> str:
+    d = os.environ.get("LINAC_GB300_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "linac_gb300")
+    return os.path.join(d, "autotune.json")
+
+
+def signature(shapes) -> str:
+    """Size signature of a batch: count, mean and max rows / columns, bucketed."""
+    ms = np.array([s[0] for s in shapes], dtype=np.float64)
+    ns = np.array([s[1] for s in shapes], dtype=np.float64)
+    def b(x):  # half-octave bucket
+        return int(round(np.log2(max(x, 1.0)) * 2))
+    return f"c{b(len(shapes))}-m{b(ms.mean())}-{b(ms.max())}-n{b(ns.mean())}-{b(ns.max())}"
+
+
+def _load_cache() -> dict:
+    try:
+        with open(_cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_cache(cache: dict):
+    path = _cache_path()
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + f".tmp{os.getpid()}"
+        with open(tmp, "w") as f:
+            json.dump(cache, f, indent=1)
+        os.replace(tmp, path)
+    except OSError:
+        pass
+
+
+def autotune(shapes, primes, sample: int = 96, reps: int = 2, seed: int = 0, force: bool = False):
+    """(tiles_per_cta, cand_rows) for a batch of these shapes.
+
+    Times every combination of TILE_CHOICES x CAND_CHOICES on a sample of up
+    to `sample` matrices drawn from the batch (random residues), keeps the
+    fastest and caches it under the batch's size signature.
+    """
+    key = signature(shapes)
+    cache = _load_cache()
+    if not force and key in cache:
+        v = cache[key]
+        return int(v["tiles_per_cta"]), int(v["cand_rows"])
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(len(shapes), size=min(sample, len(shapes)), replace=False)
+    sub_shapes = [shapes[i] for i in idx]
+    sub_primes = [int(primes[i]) for i in idx]
+    mats = [rng.integers(0, p, size=s, dtype=np.uint64).astype(np.uint32) for s, p in zip(sub_shapes, sub_primes)]
+    best, timings = None, {}
+    for tpc in TILE_CHOICES:
+        for cand in CAND_CHOICES:
+            plan = BatchPlan(sub_shapes, sub_primes, tpc, cand)
+            try:
+                plan.upload_packed(plan.pack(mats))
+                plan.run()
+                plan.finish()
+                t0 = time.perf_counter()
+                for _ in range(reps):  # each run re-reads the uploaded inputs
+                    plan.run()
+                plan.stream.synchronize()
+                dt = (time.perf_counter() - t0) / reps
+            finally:
+                plan.close()
+            timings[f"{tpc}x{cand}"] = dt
+            if best is None or dt < best[0]:
+                best = (dt, tpc, cand)
+    cache[key] = {"tiles_per_cta": best[1], "cand_rows": best[2], "seconds": best[0], "timings": timings}
+    _store_cache(cache)
+    return best[1], best[2]

@@ -1,0 +1,399 @@
+// Candidate-block panel kernels (device code shared by cand_panel.cu and
+// batch.cu).  See cand_panel.cu for the method.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_bf16.h>
+
+#include "rref_internal.cuh"
+
+namespace lnc {
+
+struct Mont32 {
+    uint32_t p, pinv, r2;  // pinv = -p^-1 mod 2^32, r2 = 2^64 mod p
+    uint64_t mu;           // Barrett constant (p = 2 path)
+    __device__ Mont32(const decltype(CandArgs::M)& c) : p(c.p), pinv(c.pinv), r2(c.r2), mu(c.mu) {}
+    __device__ __forceinline__ uint32_t mont(uint64_t t) const {
+        const uint32_t m = (uint32_t)t * pinv;
+        const uint64_t mp = (uint64_t)m * p;
+        // (t + m p) / 2^32: the low words cancel, carry iff low(t) != 0
+        const uint64_t u = (t >> 32) + (mp >> 32) + (((uint32_t)t != 0u) ? 1ull : 0ull);
+        return (uint32_t)(u >= p ? u - p : u);
+    }
+    __device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b) const { return mont((uint64_t)a * b); }
+    __device__ __forceinline__ uint32_t to_mont(uint32_t a) const { return montmul(a, r2); }
+    __device__ __forceinline__ uint32_t from_mont(uint32_t a) const { return mont((uint64_t)a); }
+    __device__ __forceinline__ uint32_t barrett(uint64_t x) const {
+        uint64_t q = __umul64hi(x, mu);
+        uint64_t r = x - q * (uint64_t)p;
+        r = (r >= p) ? r - p : r;
+        r = (r >= p) ? r - p : r;
+        return (uint32_t)r;
+    }
+    __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return a >= b ? a - b : a + (p - b); }
+};
+
+template <bool MONT>
+__device__ __forceinline__ uint32_t cp_inverse(const Mont32& M, uint32_t a) {
+    if constexpr (MONT) {
+        uint32_t x = M.to_mont(a), r = M.to_mont(1u);
+        uint64_t e = (uint64_t)M.p - 2;
+        while (e) {
+            if (e & 1) r = M.montmul(r, x);
+            x = M.montmul(x, x);
+            e >>= 1;
+        }
+        return M.from_mont(r);
+    } else {
+        return 1u;  // p = 2: the only non-zero residue is its own inverse
+    }
+}
+
+// Arithmetic policies of the candidate panel.  `prep` turns a normalised
+// pivot-row value into the form its multiplier uses, `mulp(f, prep(v))` is
+// f * v mod p, `mul` multiplies two ordinary residues.
+struct ArithSmall {  // odd p < 2^31: 32-bit Montgomery, reductions by unsigned min
+    Mont32 M;
+    __device__ ArithSmall(const decltype(CandArgs::M)& c) : M(c) {}
+    __device__ __forceinline__ uint32_t red(uint64_t t) const {
+        const uint32_t lo = (uint32_t)t, hi = (uint32_t)(t >> 32);
+        const uint32_t mh = __umulhi(lo * M.pinv, M.p);
+        const uint32_t u = hi + mh + (lo != 0u ? 1u : 0u);  // < 2p < 2^32
+        return min(u, u - M.p);
+    }
+    __device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b) const { return red((uint64_t)a * b); }
+    __device__ __forceinline__ uint32_t prep(uint32_t v) const { return montmul(v, M.r2); }
+    __device__ __forceinline__ uint32_t mulp(uint32_t f, uint32_t vp) const { return montmul(f, vp); }
+    __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return montmul(montmul(a, b), M.r2); }
+    __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const {
+        const uint32_t d = a - b;
+        return min(d, d + M.p);
+    }
+    __device__ __forceinline__ uint32_t inverse(uint32_t a) const {
+        uint32_t x = montmul(a, M.r2), r = montmul(1u, M.r2);
+        uint32_t e = M.p - 2;
+        while (e) {
+            if (e & 1u) r = montmul(r, x);
+            x = montmul(x, x);
+            e >>= 1;
+        }
+        return red((uint64_t)r);
+    }
+};
+struct ArithMont {  // odd p >= 2^31
+    Mont32 M;
+    __device__ ArithMont(const decltype(CandArgs::M)& c) : M(c) {}
+    __device__ __forceinline__ uint32_t prep(uint32_t v) const { return M.to_mont(v); }
+    __device__ __forceinline__ uint32_t mulp(uint32_t f, uint32_t vp) const { return M.montmul(f, vp); }
+    __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return M.montmul(M.to_mont(a), b); }
+    __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
+    __device__ __forceinline__ uint32_t inverse(uint32_t a) const { return cp_inverse<true>(M, a); }
+};
+struct ArithTwo {  // p = 2
+    Mont32 M;
+    __device__ ArithTwo(const decltype(CandArgs::M)& c) : M(c) {}
+    __device__ __forceinline__ uint32_t prep(uint32_t v) const { return v; }
+    __device__ __forceinline__ uint32_t mulp(uint32_t f, uint32_t vp) const { return M.barrett((uint64_t)f * vp); }
+    __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return M.barrett((uint64_t)a * b); }
+    __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
+    __device__ __forceinline__ uint32_t inverse(uint32_t) const { return 1u; }
+};
+
+// block-wide exclusive scan of a 0/1 flag (blockDim.x <= 1024); returns the
+// prefix, writes the total to *total (shared)
+__device__ __forceinline__ int block_scan_flag(int flag, int* s_warp, int* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned ballot = __ballot_sync(0xffffffffu, flag);
+    const int in_warp = __popc(ballot & ((1u << lane) - 1u));
+    if (lane == 0) s_warp[warp] = __popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int w = 0; w < nw; ++w) {
+            const int v = s_warp[w];
+            s_warp[w] = acc;
+            acc += v;
+        }
+        *total = acc;
+    }
+    __syncthreads();
+    const int r = s_warp[warp] + in_warp;
+    __syncthreads();
+    return r;
+}
+
+template <class Arith>
+__device__ __forceinline__ void cand_body(const CandArgs& a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int bw = a.bw;
+    // column-major block, odd pitch: a column (fixed c, consecutive rows) and a
+    // row (fixed i, consecutive columns) are both free of bank conflicts
+    const int LDT = a.smax | 1;
+    uint32_t* tile = (uint32_t*)smem_raw;                 // [bw][LDT]
+    uint32_t* nprM = tile + (size_t)LDT * kMaxPanel;      // [kMaxPanel]
+    uint32_t* fcol = nprM + kMaxPanel;                    // [256]
+    __shared__ int s_cand[256];
+    __shared__ uint8_t s_isp[256];
+    __shared__ int s_pr[kMaxPanel], s_pc[kMaxPanel];
+    __shared__ int s_warp[32];
+    __shared__ int s_n, s_total, s_next;
+    __shared__ int s_npi;           // look-ahead: pivot row of the next column (-1: none)
+    __shared__ uint32_t s_ninv;     // and the inverse of its entry
+    const Arith ar(a.M);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = kCandThreads / 32;
+
+    if (tid == 0) {
+        *a.missed = 0;
+        s_next = *a.next_row;
+    }
+    // ---- candidate rows: keep the old ones that are still eligible, refill in row order
+    {
+        const int n0 = *a.cand_n;
+        int r = -1, keep = 0;
+        if (tid < n0) {
+            r = a.cand[tid];
+            keep = !a.row_used[r];
+        }
+        const int pos = block_scan_flag(keep, s_warp, &s_total);
+        if (keep) s_cand[pos] = r;
+        if (tid == 0) s_n = s_total;
+        __syncthreads();
+    }
+    while (s_n < a.smax && s_next < a.m) {
+        const int base = s_next;
+        const int r = base + tid;
+        const int e = (r < a.m) ? !a.row_used[r] : 0;
+        const int pos = block_scan_flag(e, s_warp, &s_total);
+        const int need = a.smax - s_n;
+        if (e && pos < need) s_cand[s_n + pos] = r;
+        if (e && pos == need - 1) s_next = r + 1;  // filled: resume after the last row taken
+        __syncthreads();
+        if (tid == 0) {
+            if (s_total < need) {
+                s_n += s_total;
+                s_next = min((int64_t)base + (int64_t)blockDim.x, a.m);
+            } else {
+                s_n += need;
+            }
+        }
+        __syncthreads();
+    }
+    const int n = s_n;
+    // ---- load the candidate block
+    for (int i = warp; i < n; i += NW) {
+        const uint32_t* src = a.A + (int64_t)s_cand[i] * a.lda + a.j0;
+        for (int c = lane; c < bw; c += 32) tile[(size_t)c * LDT + i] = src[c];
+    }
+    for (int i = tid; i < 256; i += blockDim.x) s_isp[i] = 0;
+    __syncthreads();
+
+    // ---- Gauss-Jordan on the block, transform kept in the pivot columns.
+    // Look-ahead: while warps 1.. eliminate column c's pivot from the rest of the
+    // block, warp 0 first brings column c+1 up to date, picks its pivot row and
+    // computes the inverse, so the serial inverse overlaps the bulk update.
+    // Lanes run over rows, so each lane keeps its rows' multipliers in registers.
+    constexpr int RPL = (kCandRows + 31) / 32;  // rows per lane (n <= kCandRows)
+    auto pick_pivot = [&](int col, int exclude) {
+        // warp 0: first candidate row, not a pivot row and not `exclude`, with a
+        // non-zero entry in column `col`; lane 0 then computes its inverse
+        int found = -1;
+        const uint32_t* colp = tile + (size_t)col * LDT;
+        for (int base = 0; base < n && found < 0; base += 32) {
+            const int i = base + lane;
+            const bool ok = i < n && !s_isp[i] && i != exclude && colp[i] != 0u;
+            const unsigned b = __ballot_sync(0xffffffffu, ok);
+            if (b) found = base + __ffs(b) - 1;
+        }
+        if (lane == 0) {
+            s_npi = found;
+            s_ninv = (found >= 0) ? ar.inverse(colp[found]) : 0u;
+        }
+    };
+    if (warp == 0) pick_pivot(0, -1);
+    __syncthreads();
+    int k = 0;
+    for (int c = 0; c < bw; ++c) {
+        const int pi = s_npi;
+        const uint32_t inv = s_ninv;
+        if (pi < 0) {
+            // column c has no pivot: nothing changes, look at column c + 1
+            __syncthreads();
+            if (warp == 0 && c + 1 < bw) pick_pivot(c + 1, -1);
+            __syncthreads();
+            continue;
+        }
+        // normalised pivot row (its column c holds the inverse: the transform) and
+        // the multipliers of every other row
+        for (int cc = tid; cc < bw; cc += blockDim.x) {
+            uint32_t* e = tile + (size_t)cc * LDT + pi;
+            const uint32_t v = (cc == c) ? inv : ar.mul(*e, inv);
+            nprM[cc] = ar.prep(v);
+            *e = v;
+        }
+        for (int i = tid; i < n; i += blockDim.x) fcol[i] = (i == pi) ? 0u : tile[(size_t)c * LDT + i];
+        __syncthreads();
+        // this lane's rows and their multipliers (0 for the pivot row and absent rows)
+        uint32_t fr[RPL];
+#pragma unroll
+        for (int j = 0; j < RPL; ++j) {
+            const int i = lane + 32 * j;
+            fr[j] = (i < n) ? fcol[i] : 0u;
+        }
+        if (warp == 0) {
+            if (c + 1 < bw) {
+                uint32_t* colp = tile + (size_t)(c + 1) * LDT;
+                const uint32_t vp = nprM[c + 1];
+#pragma unroll
+                for (int j = 0; j < RPL; ++j) {
+                    const int i = lane + 32 * j;
+                    if (fr[j] != 0u) colp[i] = ar.sub(colp[i], ar.mulp(fr[j], vp));
+                }
+                __syncwarp();
+                pick_pivot(c + 1, pi);
+            }
+        } else {
+            // target columns: right of c + 1, then the transform columns (earlier
+            // pivot columns and c).  Earlier columns without a pivot are zero in the
+            // pivot row and stay as they are.
+            const int nright = bw - c - 2 > 0 ? bw - c - 2 : 0;
+            const int ntarget = nright + k + 1;
+            for (int t = warp - 1; t < ntarget; t += NW - 1) {
+                const int cc = (t < nright) ? c + 2 + t : ((t - nright < k) ? s_pc[t - nright] : c);
+                uint32_t* colp = tile + (size_t)cc * LDT;
+                const uint32_t vp = nprM[cc];
+                const bool zero_first = (cc == c);
+#pragma unroll
+                for (int j = 0; j < RPL; ++j) {
+                    const int i = lane + 32 * j;
+                    if (fr[j] != 0u) {
+                        const uint32_t x = zero_first ? 0u : colp[i];
+                        colp[i] = ar.sub(x, ar.mulp(fr[j], vp));
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            s_pr[k] = pi;
+            s_pc[k] = c;
+            s_isp[pi] = 1;
+        }
+        ++k;
+        __syncthreads();
+    }
+
+    // ---- outputs
+    const int64_t rank0 = *a.rank;
+    for (int idx = tid; idx < kMaxPanel * kMaxPanel; idx += blockDim.x) {
+        const int t = idx / kMaxPanel, u = idx % kMaxPanel;
+        a.X[idx] = (t < k && u < k) ? tile[(size_t)s_pc[u] * LDT + s_pr[t]] : 0u;
+    }
+    for (int t = tid; t < k; t += blockDim.x) {
+        const int r = s_cand[s_pr[t]];
+        a.panel_rows[t] = r;
+        a.panel_cols[t] = s_pc[t];
+        a.piv_row[rank0 + t] = r;
+        a.piv_col[rank0 + t] = a.j0 + s_pc[t];
+        a.row_used[r] = 1;
+        a.panel_mark[r] = (a.gen << 8) | (t + 1);
+    }
+    if (tid < 4) {
+        uint32_t mask = 0u;
+        for (int t = 0; t < k; ++t)
+            if ((s_pc[t] >> 5) == tid) mask |= 1u << (s_pc[t] & 31);
+        a.pivmask[tid] = mask;
+    }
+    {
+        const int keep = (tid < n) ? !s_isp[tid] : 0;
+        const int pos = block_scan_flag(keep, s_warp, &s_total);
+        if (keep) a.cand[pos] = s_cand[tid];
+        if (tid == 0) {
+            *a.cand_n = s_total;
+            *a.next_row = s_next;
+            *a.panel_k = k;
+            *a.rank = rank0 + k;
+        }
+    }
+}
+
+template <class Arith>
+static __global__ void __launch_bounds__(kCandThreads, 1) cand_panel_kernel(const __grid_constant__ CandArgs a) {
+    cand_body<Arith>(a);
+}
+
+// G operand of E = G X, as four K-major digit planes: G[o, t] = -A[o, j0 + c_t]
+// for rows that are not pivot rows of this panel, G[prow_t, :] = e_t.
+__device__ __forceinline__ void split4(uint32_t x, uint32_t p, __nv_bfloat16 (&d)[4]) {
+    int32_t v = (x > (p >> 1)) ? (int32_t)((int64_t)x - (int64_t)p) : (int32_t)x;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int32_t di = ((v + 128) & 255) - 128;
+        d[i] = __float2bfloat16_rn((float)di);
+        v = (v - di) >> 8;
+    }
+    d[3] = __float2bfloat16_rn((float)v);
+}
+
+__device__ __forceinline__ void split_g_body(const uint32_t* A, int64_t lda, int64_t m, int m_pad, int64_t j0,
+                                             uint32_t p, const int32_t* panel_k, const int32_t* panel_cols,
+                                             const int32_t* panel_mark, int gen, __nv_bfloat16* EL) {
+    const int k = *panel_k;
+    if (k == 0) return;
+    const size_t plane = (size_t)m_pad * kMaxPanel;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)m_pad * kMaxPanel;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / kMaxPanel;
+        const int t = (int)(idx - r * kMaxPanel);
+        uint32_t v = 0u;
+        if (r < m && t < k) {
+            const int mk = panel_mark[r];
+            if ((mk >> 8) == gen) {
+                v = ((mk & 255) - 1 == t) ? 1u : 0u;
+            } else {
+                const uint32_t x = A[r * lda + j0 + panel_cols[t]];
+                v = x ? p - x : 0u;
+            }
+        }
+        __nv_bfloat16 d[4];
+        split4(v, p, d);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) EL[i * plane + idx] = d[i];
+    }
+}
+
+// After the update every remaining (non-pivot) row must be zero in the
+// panel's non-pivot columns; a non-zero entry means the candidate block missed
+// a pivot.
+__device__ __forceinline__ void check_missed_body(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, int bw,
+                                                  const uint8_t* row_used, const uint32_t* pivmask, int* missed) {
+    __shared__ uint32_t s_mask[4];
+    if (threadIdx.x < 4) s_mask[threadIdx.x] = pivmask[threadIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int bad = 0;
+    for (int64_t r = wid; r < m; r += nw) {
+        if (row_used[r]) continue;
+        const uint32_t* row = A + r * lda + j0;
+        for (int c = lane; c < bw; c += 32)
+            if (!((s_mask[c >> 5] >> (c & 31)) & 1u) && row[c] != 0u) bad = 1;
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(missed, 1);
+}
+
+static __global__ void split_g_kernel(const uint32_t* A, int64_t lda, int64_t m, int m_pad, int64_t j0, uint32_t p,
+                                      const int32_t* panel_k, const int32_t* panel_cols, const int32_t* panel_mark,
+                                      int gen, __nv_bfloat16* EL) {
+    split_g_body(A, lda, m, m_pad, j0, p, panel_k, panel_cols, panel_mark, gen, EL);
+}
+
+static __global__ void check_missed_kernel(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, int bw,
+                                           const uint8_t* row_used, const uint32_t* pivmask, int* missed) {
+    check_missed_body(A, lda, m, j0, bw, row_used, pivmask, missed);
+}
+
+}  // namespace lnc

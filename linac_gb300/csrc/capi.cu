@@ -199,6 +199,14 @@ int load_matrix_dispatch(int dtype, int64_t n_rows, int64_t n_cols, int64_t basi
                          uint64_t p, const void* bases, const uint32_t* lind, void* out, int64_t ldo,
                          cudaStream_t s);
 
+struct BatchPlan;
+int batch_plan_create(const lnc_batch_matrix* mats, int64_t count, int tpc, int smax, cudaStream_t s,
+                      BatchPlan** out);
+int batch_run(BatchPlan* P, cudaStream_t s);
+int batch_finish(BatchPlan* P, cudaStream_t s, int64_t* n_redo);
+void batch_destroy(BatchPlan* P);
+size_t batch_plan_bytes(BatchPlan* P);
+
 }  // namespace lnc
 
 using namespace lnc;
@@ -465,6 +473,43 @@ int lnc_load_matrix_host(int dtype, int64_t n_rows, int64_t n_cols, int64_t basi
     cudaFreeAsync(dout, s);
     e = cudaStreamSynchronize(s);
     if (!rc && e != cudaSuccess) rc = cuda_status(e, "loader");
+    return rc;
+}
+
+int lnc_batch_plan_create(int dtype, const lnc_batch_matrix* mats, int64_t count, int tiles_per_cta, int cand_rows,
+                          void* stream, void** plan) {
+    if (dtype != LNC_U32) { set_error("the batched RREF serves 32-bit residues (LNC_U32)"); return LNC_ERR_UNSUPPORTED; }
+    if (!mats || !plan) { set_error("null argument"); return LNC_ERR_INVALID; }
+    BatchPlan* P = nullptr;
+    int rc = batch_plan_create(mats, count, tiles_per_cta, cand_rows, (cudaStream_t)stream, &P);
+    *plan = rc ? nullptr : (void*)P;
+    return rc;
+}
+
+int lnc_batch_plan_run(void* plan, void* stream) {
+    if (!plan) { set_error("null plan"); return LNC_ERR_INVALID; }
+    return batch_run((BatchPlan*)plan, (cudaStream_t)stream);
+}
+
+int lnc_batch_plan_finish(void* plan, void* stream, int64_t* n_redo) {
+    if (!plan) { set_error("null plan"); return LNC_ERR_INVALID; }
+    return batch_finish((BatchPlan*)plan, (cudaStream_t)stream, n_redo);
+}
+
+int64_t lnc_batch_plan_bytes(void* plan) { return (int64_t)batch_plan_bytes((BatchPlan*)plan); }
+
+int lnc_batch_plan_destroy(void* plan) {
+    batch_destroy((BatchPlan*)plan);
+    return LNC_OK;
+}
+
+int lnc_rref_batch_device(int dtype, const lnc_batch_matrix* mats, int64_t count, void* stream, int /*flags*/) {
+    void* plan = nullptr;
+    int rc = lnc_batch_plan_create(dtype, mats, count, 0, 0, stream, &plan);
+    if (rc) return rc;
+    rc = lnc_batch_plan_run(plan, stream);
+    if (!rc) rc = lnc_batch_plan_finish(plan, stream, nullptr);
+    lnc_batch_plan_destroy(plan);
     return rc;
 }
 

@@ -31,365 +31,16 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
+#include <algorithm>
 
 #include <cuda.h>
 #include <cuda_bf16.h>
 
-#include "rref_internal.cuh"
-#include "tc_ptx.cuh"
+#include "tc_kernels.cuh"
 
 namespace lnc {
 namespace tc {
-
-constexpr int BM = 128;                 // tile rows (TMEM lanes)
-constexpr int BN = 32;                  // output columns per tile
-constexpr int LIMBS = 4;                // base-256 digits per residue
-constexpr int KMAX = 128;               // contraction depth (panel width)
-constexpr int KC = 64;                  // K per stage: one 128-byte swizzle row of BF16
-constexpr int NKC = KMAX / KC;          // 2
-constexpr int GROUPS = 2 * LIMBS - 1;   // 7 weights 256^0 .. 256^6
-constexpr int B_ROWS = LIMBS * BN;      // 128 stacked digit rows per output tile (UMMA N)
-constexpr int STAGES = 4;
-constexpr int TILES_PER_CTA = 16;
-constexpr int EPI_WARPS = 8;            // two per TMEM lane quarter, 16 columns each
-constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t ACC_STRIDE = 256;    // two accumulators of GROUPS * BN = 224 columns
-constexpr uint32_t A_TILE_BYTES = BM * KC * 2;      // 16 KB
-constexpr uint32_t B_TILE_BYTES = B_ROWS * KC * 2;  // 16 KB
-constexpr uint32_t A_BYTES = LIMBS * NKC * A_TILE_BYTES;  // 128 KB
-constexpr uint32_t SMEM_BYTES = A_BYTES + STAGES * B_TILE_BYTES + 1024 /*barriers*/ + 1024 /*align*/;
-// exact float -> int for |x| < 2^22: x + 1.5 * 2^23 has unit spacing
-constexpr float MAGIC_F = 12582912.0f;
-constexpr int32_t MAGIC_I = 0x4B400000;
-
-struct TcParams {
-    uint32_t* C;            // trailing block base: A + j1
-    int64_t ldc;
-    int64_t m;
-    int64_t N;
-    int m_pad;              // rows per digit plane in the E operand
-    int n_tiles;            // 64-column tiles covering N
-    const int32_t* panel_k;
-    FieldU32 f;
-    int32_t w[GROUPS];      // 256^s mod p, centred
-    uint64_t off;           // multiple of p >= 2^59 (makes the 64-bit sum non-negative)
-    int overwrite;          // 1: C <- E * B (C is not read), 0: C <- C + E * B
-    uint32_t pinv;          // -p^-1 mod 2^32 (Montgomery reduction of the epilogue sum)
-    int* err;
-    int* status;
-};
-
-__device__ __forceinline__ void split_digits(uint32_t x, uint32_t p, uint32_t half, __nv_bfloat16 (&d)[LIMBS]) {
-    int32_t v = (x > half) ? (int32_t)((int64_t)x - (int64_t)p) : (int32_t)x;
-#pragma unroll
-    for (int i = 0; i < LIMBS - 1; ++i) {
-        const int32_t di = ((v + 128) & 255) - 128;
-        d[i] = __float2bfloat16_rn((float)di);
-        v = (v - di) >> 8;
-    }
-    d[LIMBS - 1] = __float2bfloat16_rn((float)v);  // |v| <= 128
-}
-
-// E (m x ldE residues, columns >= k are zero) -> four K-major digit planes of
-// m_pad x 128 BF16.
-__global__ void split_e_kernel(const uint32_t* E, int64_t ldE, int b, int64_t m, int m_pad, uint32_t p,
-                               const int32_t* panel_k, __nv_bfloat16* EL) {
-    const int k = *panel_k;
-    if (k == 0) return;
-    const uint32_t half = p >> 1;
-    const size_t plane = (size_t)m_pad * KMAX;
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)m_pad * KMAX;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = idx / KMAX;
-        const int t = (int)(idx - r * KMAX);
-        uint32_t x = (r < m && t < k && t < b) ? E[r * ldE + t] : 0u;
-        __nv_bfloat16 d[LIMBS];
-        split_digits(x, p, half, d);
-#pragma unroll
-        for (int i = 0; i < LIMBS; ++i) EL[i * plane + idx] = d[i];
-    }
-}
-
-// Pivot rows of the trailing block -> stacked digit rows (one CTA per 64-column
-// tile), zeroing those rows in C.
-__global__ void __launch_bounds__(256) gather_split_b_kernel(uint32_t* C, int64_t ldc, int64_t N,
-                                                             const int32_t* panel_rows, const int32_t* panel_k,
-                                                             uint32_t p, __nv_bfloat16* BS, int zero_src) {
-    __shared__ uint32_t s[KMAX][BN + 1];
-    const int k = *panel_k;
-    if (k == 0) return;
-    const int tile = blockIdx.x;
-    const int64_t c0 = (int64_t)tile * BN;
-    const uint32_t half = p >> 1;
-    for (int idx = threadIdx.x; idx < KMAX * BN; idx += blockDim.x) {
-        const int t = idx / BN, cc = idx % BN;
-        uint32_t v = 0;
-        if (t < k && c0 + cc < N) {
-            uint32_t* src = C + (int64_t)(panel_rows ? panel_rows[t] : t) * ldc + c0 + cc;
-            v = *src;
-            if (zero_src) *src = 0u;
-        }
-        s[t][cc] = v;
-    }
-    __syncthreads();
-    // row (i, cc) of this tile's stacked block holds digit i of column cc for t = 0..127
-    __nv_bfloat16* dst = BS + (size_t)tile * B_ROWS * KMAX;
-    for (int idx = threadIdx.x; idx < BN * KMAX; idx += blockDim.x) {
-        const int cc = idx / KMAX, t = idx % KMAX;
-        __nv_bfloat16 d[LIMBS];
-        split_digits(s[t][cc], p, half, d);
-#pragma unroll
-        for (int i = 0; i < LIMBS; ++i) dst[((size_t)i * BN + cc) * KMAX + t] = d[i];
-    }
-}
-
-__device__ __forceinline__ void flag_error(const TcParams& P, volatile int* cta_err) {
-    *cta_err = 1;
-    atomicExch(P.err, LNC_ERR_TIMEOUT);
-    atomicExch(P.status, LNC_ERR_TIMEOUT);
-}
-
-// v mod p for the epilogue sum v < 2^60: Montgomery (v 2^-32; the weights
-// already carry the factor 2^32) when 2^30 <= p < 2^31, else Barrett.
-template <bool REDC>
-__device__ __forceinline__ uint32_t reduce_sum(const FieldU32& f, uint32_t pinv, uint64_t v) {
-    if constexpr (REDC) {
-        const uint32_t lo = (uint32_t)v;
-        const uint32_t u = (uint32_t)(v >> 32) + __umulhi(lo * pinv, f.p) + (lo != 0u ? 1u : 0u);  // < 2p
-        return min(u, u - f.p);
-    } else {
-        return f.reduce64(v);
-    }
-}
-
-// REDC: 2^30 <= p < 2^31, the weights carry an extra factor 2^32 and the
-// 64-bit sum is reduced by one Montgomery step; otherwise Barrett.
-template <bool REDC>
-__global__ void __launch_bounds__(THREADS, 1)
-    limb_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                     const TcParams P) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // 1024-byte alignment for the 128-byte swizzle atoms
-    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    unsigned char* sA = smem;                         // [LIMBS][NKC][BM x KC]
-    unsigned char* sB = smem + A_BYTES;               // [STAGES][B_ROWS x KC]
-    uint64_t* bars = (uint64_t*)(sB + STAGES * B_TILE_BYTES);
-    uint64_t* a_full = bars + 0;
-    uint64_t* b_full = bars + 1;                  // [STAGES]
-    uint64_t* b_empty = bars + 1 + STAGES;        // [STAGES]
-    uint64_t* acc_full = bars + 1 + 2 * STAGES;   // [2]
-    uint64_t* acc_empty = bars + 3 + 2 * STAGES;  // [2]
-    uint64_t* drain = bars + 5 + 2 * STAGES;
-    uint32_t* s_tmem = (uint32_t*)(bars + 6 + 2 * STAGES);
-    __shared__ volatile int s_err;
-
-    const int k = *P.panel_k;  // written by an earlier kernel: identical in every thread
-    if (k == 0) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rb = blockIdx.y;
-    const int t0 = blockIdx.x * TILES_PER_CTA;
-    const int t1 = min(P.n_tiles, t0 + TILES_PER_CTA);
-    const int ntiles = t1 - t0;
-    const int nkc = (k > KC) ? 2 : 1;  // skip the second K chunk when it is all zero
-
-    if (threadIdx.x == 0) {
-        s_err = (ld_volatile_i32(P.err) != 0) ? 1 : 0;  // an earlier kernel of this call failed
-        ptx::mbar_init(a_full, 1);
-        for (int s = 0; s < STAGES; ++s) {
-            ptx::mbar_init(&b_full[s], 1);
-            ptx::mbar_init(&b_empty[s], 1);
-        }
-        for (int b = 0; b < 2; ++b) {
-            ptx::mbar_init(&acc_full[b], 1);
-            ptx::mbar_init(&acc_empty[b], EPI_WARPS);
-        }
-        ptx::mbar_init(drain, 1);
-        ptx::fence_mbar_init();
-    }
-    if (warp == 1) {
-        ptx::tmem_alloc(s_tmem, TMEM_COLS);
-        ptx::tmem_relinquish();
-    }
-    ptx::tc_fence_before();
-    __syncthreads();
-    ptx::tc_fence_after();
-    const uint32_t tmem = *s_tmem;
-
-    if (warp == 0) {
-        // ------------------------------------------------------------ producer
-        if (lane == 0) {
-            ptx::prefetch_tmap(&tmA);
-            ptx::prefetch_tmap(&tmB);
-            ptx::mbar_expect_tx(a_full, LIMBS * nkc * A_TILE_BYTES);
-            for (int i = 0; i < LIMBS; ++i)
-                for (int kc = 0; kc < nkc; ++kc)
-                    ptx::tma_load_2d(sA + (i * NKC + kc) * A_TILE_BYTES, &tmA, a_full, kc * KC,
-                                     i * P.m_pad + rb * BM);
-            int it = 0;
-            int issued_round[STAGES];
-            for (int st = 0; st < STAGES; ++st) issued_round[st] = -1;
-            for (int t = 0; t < ntiles && !s_err; ++t) {
-                for (int kc = 0; kc < nkc; ++kc, ++it) {
-                    const int st = it % STAGES, round = it / STAGES;
-                    if (!ptx::mbar_wait(&b_empty[st], (round & 1) ^ 1, &s_err)) { flag_error(P, &s_err); break; }
-                    ptx::mbar_expect_tx(&b_full[st], B_TILE_BYTES);
-                    ptx::tma_load_2d(sB + st * B_TILE_BYTES, &tmB, &b_full[st], kc * KC, (t0 + t) * B_ROWS);
-                    issued_round[st] = round;
-                }
-            }
-            // never leave with copies in flight: wait (bounded) for every load issued
-            const long long lim = kSpinLimitCycles / 4;
-            ptx::mbar_wait_nocancel(a_full, 0, lim);
-            for (int st = 0; st < STAGES; ++st)
-                if (issued_round[st] >= 0) ptx::mbar_wait_nocancel(&b_full[st], issued_round[st] & 1, lim);
-        }
-    } else if (warp == 1) {
-        // ------------------------------------------------------------ MMA issuer
-        if (lane == 0) {
-            constexpr uint32_t idesc = ptx::umma_idesc_bf16(BM, B_ROWS);
-            const uint32_t a_base = ptx::smem_u32(sA);
-            const uint32_t b_base = ptx::smem_u32(sB);
-            bool ok = ptx::mbar_wait(a_full, 0, &s_err);
-            if (!ok) flag_error(P, &s_err);
-            int it = 0;
-            for (int t = 0; t < ntiles && ok; ++t) {
-                const int buf = t & 1;
-                if (!ptx::mbar_wait(&acc_empty[buf], (t >> 1) & 1, &s_err)) { flag_error(P, &s_err); break; }
-                ptx::tc_fence_after();
-                const uint32_t dbase = tmem + ACC_STRIDE * buf;
-                for (int kc = 0; kc < nkc && ok; ++kc, ++it) {
-                    const int st = it % STAGES, round = it / STAGES;
-                    if (!ptx::mbar_wait(&b_full[st], round & 1, &s_err)) { flag_error(P, &s_err); ok = false; break; }
-                    ptx::tc_fence_after();
-#pragma unroll
-                    for (int ks = 0; ks < KC / 16; ++ks) {
-                        const uint64_t bdesc = ptx::umma_desc_sw128(b_base + st * B_TILE_BYTES + ks * 32);
-#pragma unroll
-                        for (int i = 0; i < LIMBS; ++i) {
-                            const uint64_t adesc =
-                                ptx::umma_desc_sw128(a_base + (i * NKC + kc) * A_TILE_BYTES + ks * 32);
-                            ptx::umma_bf16(dbase + (uint32_t)(BN * i), adesc, bdesc, idesc, 1u);
-                        }
-                    }
-                    ptx::umma_commit(&b_empty[st]);  // stage reusable once these UMMAs finish
-                }
-                if (ok) ptx::umma_commit(&acc_full[buf]);
-            }
-            // all issued UMMAs complete before the TMEM is released
-            ptx::umma_commit(drain);
-            ptx::mbar_wait_nocancel(drain, 0, kSpinLimitCycles / 4);
-        }
-    } else {
-        // ------------------------------------------------------------ epilogue
-        const int ew = warp - 2;            // 0 .. EPI_WARPS-1
-        const int q = warp & 3;             // TMEM lane quarter this warp may access
-        const int half = ew >> 2;           // which 16 of the tile's 32 columns
-        const int64_t row = (int64_t)rb * BM + q * 32 + lane;
-        const uint32_t t_lane = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(16 * half);
-        const FieldU32 f = P.f;
-        const bool row_ok = row < P.m;
-        // zero both accumulators (this warp's lanes and columns)
-        for (int b = 0; b < 2; ++b) {
-            for (int g = 0; g < GROUPS; ++g) ptx::tmem_st16_zero(t_lane + ACC_STRIDE * b + BN * g);
-        }
-        ptx::tmem_st_wait();
-        ptx::tc_fence_before();
-        __syncwarp();
-        if (lane == 0) {
-            ptx::mbar_arrive(&acc_empty[0]);
-            ptx::mbar_arrive(&acc_empty[1]);
-        }
-        int64_t wsum = 0;  // sum of the weights: removes the magic offset in one step
-#pragma unroll
-        for (int g = 0; g < GROUPS; ++g) wsum += P.w[g];
-        const uint64_t bias = P.off - (uint64_t)((int64_t)MAGIC_I * wsum);
-        for (int t = 0; t < ntiles; ++t) {
-            const int buf = t & 1;
-            const int64_t col0 = (int64_t)(t0 + t) * BN + 16 * half;
-            uint32_t* crow = P.C + (row_ok ? row : 0) * P.ldc + col0;
-            const int ncols = (int)((P.N - col0) < 16 ? (P.N - col0) : 16);
-            const bool vec = row_ok && ncols == 16 && ((((uintptr_t)crow) & 15) == 0);
-            uint32_t old[16];
-            if (P.overwrite) {
-#pragma unroll
-                for (int c = 0; c < 16; ++c) old[c] = 0u;
-            } else if (vec) {
-#pragma unroll
-                for (int c = 0; c < 16; c += 4) {
-                    const uint4 v = *(const uint4*)(crow + c);
-                    old[c] = v.x; old[c + 1] = v.y; old[c + 2] = v.z; old[c + 3] = v.w;
-                }
-            } else {
-#pragma unroll
-                for (int c = 0; c < 16; ++c) old[c] = (row_ok && c < ncols) ? crow[c] : 0u;
-            }
-            const bool got = ptx::mbar_wait(&acc_full[buf], (t >> 1) & 1, &s_err);
-            if (!__all_sync(0xffffffffu, got)) {  // warp-uniform before the aligned TMEM loads
-                if (lane == 0) flag_error(P, &s_err);
-                break;
-            }
-            ptx::tc_fence_after();
-            uint32_t d[GROUPS][16];
-#pragma unroll
-            for (int g = 0; g < GROUPS; ++g) ptx::tmem_ld16(t_lane + ACC_STRIDE * buf + BN * g, d[g]);
-            ptx::tmem_ld_wait();
-            // accumulator drained: re-zero it and hand it back to the MMA warp
-#pragma unroll
-            for (int g = 0; g < GROUPS; ++g) ptx::tmem_st16_zero(t_lane + ACC_STRIDE * buf + BN * g);
-            ptx::tmem_st_wait();
-            ptx::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&acc_empty[buf]);
-            // exact conversion: for |x| <= 2^22, x + 1.5 * 2^23 is exact and its bit pattern minus
-            // 0x4B400000 is x (full-rate FADD instead of the quarter-rate F2I).  Groups 0, 1, 5, 6 hold
-            // at most two digit products per step and stay within 2^22 for any input; groups 2-4 are
-            // checked.  The weighted sum is formed modulo 2^64; its true value lies in [0, 2^60].
-            float mx = 0.f;
-#pragma unroll
-            for (int g = 2; g <= 4; ++g)
-#pragma unroll
-                for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
-            const bool fast = mx <= 4194304.0f;
-            uint32_t res[16];
-            if (__all_sync(0xffffffffu, fast)) {
-#pragma unroll
-                for (int c = 0; c < 16; ++c) {
-                    uint64_t v = (uint64_t)bias;
-#pragma unroll
-                    for (int g = 0; g < GROUPS; ++g) {
-                        const int32_t y = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F));
-                        v += (uint64_t)((int64_t)y * (int64_t)P.w[g]);
-                    }
-                    res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
-                }
-            } else {
-#pragma unroll
-                for (int c = 0; c < 16; ++c) {
-                    uint64_t v = P.off;
-#pragma unroll
-                    for (int g = 0; g < GROUPS; ++g)
-                        v += (uint64_t)((int64_t)__float2int_rn(__uint_as_float(d[g][c])) * (int64_t)P.w[g]);
-                    res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
-                }
-            }
-            if (vec) {
-#pragma unroll
-                for (int c = 0; c < 16; c += 4)
-                    *(uint4*)(crow + c) = make_uint4(res[c], res[c + 1], res[c + 2], res[c + 3]);
-            } else if (row_ok) {
-#pragma unroll
-                for (int c = 0; c < 16; ++c)
-                    if (c < ncols) crow[c] = res[c];
-            }
-        }
-    }
-    ptx::tc_fence_before();
-    __syncthreads();
-    ptx::tc_fence_after();
-    if (warp == 1) ptx::tmem_dealloc(tmem, TMEM_COLS);
-}
-
 // ----------------------------------------------------------------------------
 // host side
 // ----------------------------------------------------------------------------
@@ -433,6 +84,15 @@ static int make_map(CUtensorMap* map, void* base, uint64_t inner, uint64_t outer
     }
     return LNC_OK;
 }
+
+}  // namespace tc
+
+int tc_make_map_bf16(CUtensorMap* map, void* base, uint64_t inner, uint64_t outer, uint32_t box_inner,
+                     uint32_t box_outer) {
+    return tc::make_map(map, base, inner, outer, box_inner, box_outer);
+}
+
+namespace tc {
 
 static int m_pad_of(int64_t m) { return (int)((m + BM - 1) / BM * BM); }
 static int n_tiles_of(int64_t n) { return (int)((n + BN - 1) / BN); }
@@ -525,6 +185,7 @@ int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t
     }
     P.err = err;
     P.status = status;
+    P.redc = redc ? 1 : 0;
     auto kern = redc ? limb_gemm_kernel<true> : limb_gemm_kernel<false>;
     LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
@@ -548,4 +209,57 @@ int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s) {
                         !t.predicated);
 }
 
+// C = A B mod p (32-bit residues, any sizes): the limb GEMM applied to
+// 128-deep slices of the contraction, the first slice overwriting C.
+int tc_matmul_modp(uint32_t p, int64_t m, int64_t k, int64_t n, const uint32_t* A, int64_t lda,
+                   const uint32_t* B, int64_t ldb, uint32_t* C, int64_t ldc, cudaStream_t s) {
+    using namespace tc;
+    if (m <= 0 || n <= 0) return LNC_OK;
+    if (k <= 0) {
+        LNC_CUDA(cudaMemset2DAsync(C, 4 * ldc, 0, 4 * n, m, s));
+        return LNC_OK;
+    }
+    if (!trailing_tc_u32_available()) { set_error("tensor-core path unavailable"); return LNC_ERR_UNSUPPORTED; }
+    const FieldU32 f = FieldU32::make(p);
+    const int64_t chunks = (k + KMAX - 1) / KMAX;
+    const size_t el = tc_el_bytes(m), bs = tc_bs_bytes(n);
+    void* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, el + bs + 1024 + 256 + sizeof(int32_t) * chunks + 16, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("matmul scratch: %s", cudaGetErrorString(e));
+        return LNC_ERR_OOM;
+    }
+    unsigned char* base = (unsigned char*)(((uintptr_t)scratch + 1023) & ~(uintptr_t)1023);
+    void* EL = base;
+    void* BS = base + el;
+    int32_t* ks = (int32_t*)(base + el + bs);
+    int* words = (int*)(ks + chunks);
+    std::vector<int32_t> hk((size_t)chunks);
+    for (int64_t c = 0; c < chunks; ++c) hk[(size_t)c] = (int32_t)std::min<int64_t>(KMAX, k - c * KMAX);
+    int rc = LNC_OK;
+    e = cudaMemcpyAsync(ks, hk.data(), sizeof(int32_t) * chunks, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(words, 0, 8, s);
+    if (e != cudaSuccess) rc = cuda_status(e, "matmul setup");
+    if (!rc) e = cudaStreamSynchronize(s);  // the chunk sizes live in pageable host memory
+    for (int64_t c = 0; c < chunks && !rc; ++c) {
+        rc = tc_split_e(A + c * KMAX, lda, KMAX, m, p, ks + c, EL, s);
+        if (!rc) rc = tc_gather_split_b(const_cast<uint32_t*>(B) + c * KMAX * ldb, ldb, n, nullptr, ks + c, p, BS,
+                                        false, s);
+        if (!rc) rc = tc_limb_gemm(f, C, ldc, m, n, ks + c, c == 0, EL, BS, n, words, words + 1, s);
+    }
+    cudaFreeAsync(scratch, s);
+    return rc;
+}
+
 }  // namespace lnc
+
+extern "C" int lnc_matmul_modp_device(int dtype, int64_t m, int64_t k, int64_t n, uint64_t p, const void* A,
+                                      int64_t lda, const void* B, int64_t ldb, void* C, int64_t ldc, void* stream) {
+    using namespace lnc;
+    if (dtype != LNC_U32) { set_error("matmul: LNC_U32 only"); return LNC_ERR_UNSUPPORTED; }
+    if (p < 2 || p > 0xFFFFFFFFull) { set_error("matmul: 2 <= p < 2^32"); return LNC_ERR_INVALID; }
+    if (lda < k || ldb < n || ldc < n) { set_error("matmul: leading dimension too small"); return LNC_ERR_INVALID; }
+    return tc_matmul_modp((uint32_t)p, m, k, n, (const uint32_t*)A, lda, (const uint32_t*)B, ldb, (uint32_t*)C, ldc,
+                          (cudaStream_t)stream);
+}

@@ -1,0 +1,96 @@
+"""GPU parity of the batched RREF (csrc/batch.cu): every matrix of an uneven
+batch with its own prime must equal the oracle bit for bit, including
+rank-deficient, tiny, wide / tall and structured matrices that make the
+candidate panels miss pivots (those are redone exhaustively)."""
+import numpy as np
+import pytest
+
+import oracle
+from linac_gb300 import workloads
+from linac_gb300.batch import BatchPlan, rref_batch
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(count, seed, m_lo=20, m_hi=700):
+    rng = np.random.default_rng(seed)
+    shapes = workloads.batch_shapes(count, rng, m_lo, m_hi)
+    mats, primes = [], []
+    for m, n, r, p in shapes:
+        mats.append(workloads.rank_deficient_modp(m, n, r, p, rng).astype(np.uint32) if r < min(m, n)
+                    else rng.integers(0, p, size=(m, n), dtype=np.uint64).astype(np.uint32))
+        primes.append(p)
+    return mats, primes
+
+
+def test_batch_uneven_primes_matches_oracle():
+    mats, primes = _batch(48, 1)
+    res, pivs = rref_batch(mats, primes, return_pivots=True, tune=False)
+    for A, p, R, pv in zip(mats, primes, res, pivs):
+        R_ref, piv_ref, _ = oracle.rref_modp(A, p)
+        assert np.array_equal(R.astype(np.uint64), R_ref)
+        assert pv == piv_ref
+
+
+def test_batch_structured_and_edge_matrices():
+    rng = np.random.default_rng(5)
+    p = 2**31 - 1
+    mats = [np.zeros((40, 30), dtype=np.uint32),                                       # zero
+            rng.integers(0, p, size=(1, 300), dtype=np.uint64).astype(np.uint32),      # one row
+            rng.integers(0, p, size=(300, 1), dtype=np.uint64).astype(np.uint32),      # one column
+            rng.integers(0, p, size=(129, 257), dtype=np.uint64).astype(np.uint32)]    # ragged
+    A = rng.integers(0, p, size=(600, 500), dtype=np.uint64).astype(np.uint32)
+    A[:300, :40] = 0  # candidate rows miss the leading pivots: exhaustive redo
+    mats.append(A)
+    primes = [p, 2**31 - 19, 3, 65521, p]
+    plan = BatchPlan([M.shape for M in mats], primes)
+    try:
+        plan.upload_packed(plan.pack(mats))
+        for _ in range(2):  # the plan re-runs on the same inputs
+            plan.run()
+            redone = plan.finish()
+            out = plan.unpack(plan.download_packed(np.empty(plan.total_bytes, dtype=np.uint8)))
+            for M, q, R in zip(mats, primes, out):
+                R_ref, _, _ = oracle.rref_modp(M, q)
+                assert np.array_equal(R.astype(np.uint64), R_ref)
+        assert redone >= 1
+    finally:
+        plan.close()
+
+
+def test_batch_single_large_and_many_small():
+    rng = np.random.default_rng(9)
+    p = 2**31 - 1
+    mats = [rng.integers(0, p, size=(1500, 1400), dtype=np.uint64).astype(np.uint32)]
+    mats += [rng.integers(0, p, size=(int(m), int(m) + 3), dtype=np.uint64).astype(np.uint32)
+             for m in rng.integers(2, 90, size=60)]
+    primes = [p] * len(mats)
+    res = rref_batch(mats, primes, tune=False)
+    for A, R in zip(mats, res):
+        R_ref, _, _ = oracle.rref_modp(A, p)
+        assert np.array_equal(R.astype(np.uint64), R_ref)
+
+
+def test_matmul_and_fill_helpers_exact():
+    import ctypes
+    from linac_gb300 import _lib
+    L = _lib.lib()
+    p = 2**31 - 19
+    rng = np.random.default_rng(3)
+    for (m, k, n) in [(300, 77, 500), (129, 300, 65), (5, 1, 3)]:
+        A = rng.integers(0, p, size=(m, k), dtype=np.uint64).astype(np.uint32)
+        B = rng.integers(0, p, size=(k, n), dtype=np.uint64).astype(np.uint32)
+        dA, dB, dC = _lib.DeviceBuffer(A.nbytes), _lib.DeviceBuffer(B.nbytes), _lib.DeviceBuffer(4 * m * n)
+        s = _lib.Stream()
+        dA.upload(A, s.handle)
+        dB.upload(B, s.handle)
+        _lib.check(L.lnc_matmul_modp_device(_lib.LNC_U32, m, k, n, p, dA.ptr, k, dB.ptr, n, dC.ptr, n, s.handle))
+        C = np.empty((m, n), dtype=np.uint32)
+        dC.download(C, s.handle)
+        assert np.array_equal(C.astype(np.uint64), oracle.matmul_modp(A, B, p))
+    d = _lib.DeviceBuffer(4 * 100000)
+    _lib.check(L.lnc_fill_uniform_modp(d.ptr, 100000, 65521, 7, _lib.LNC_U32, None))
+    x = np.empty(100000, dtype=np.uint32)
+    d.download(x)
+    # 100000 draws from 65521 values: about 51300 distinct are expected
+    assert x.max() < 65521 and 48000 < len(np.unique(x)) < 54000

@@ -55,6 +55,10 @@ WORKLOADS = {
     # a prime per matrix from the 64 largest primes below 2^31, built as B.C on the device
     "batch4096": dict(count=4096, m_lo=64, m_hi=2048, dtype="u32", batch=True),
     "batch512": dict(count=512, m_lo=64, m_hi=2048, dtype="u32", batch=True),
+    # served load+RREF stream: Poisson arrivals, a random prime below 2^31 per request, all
+    # monomials of degree <= d (d ~ U{3..8}) in 10 variables truncated to 8000 columns,
+    # rows = columns + 16 points uniform in F_p^10, non-zero uniform prefactors
+    "serve": dict(per_step=32, d_lo=3, d_hi=8, dtype="u32", serve=True),
 }
 
 
@@ -403,10 +407,75 @@ def traffic_per_launch(kernel: str):
 # ---------------------------------------------------------------------------
 # reference arm: the reference's CPU algorithm (oracle port), bounded samples
 # ---------------------------------------------------------------------------
+def _reference_sampled(args, wl):
+    """Batched / served workloads on the CPU: whole solves of the oracle (all
+    host threads) on matrices of the workload, in seeded random order, until
+    the step's time budget is spent; the rate is scaled by algorithmic work to
+    the workload's mean request."""
+    import oracle
+    from linac_gb300 import workloads
+    oracle.build()
+    rng = np.random.default_rng(99)
+    if wl.get("batch"):
+        specs = workloads.batch_shapes(wl["count"], np.random.default_rng(2024), wl["m_lo"], wl["m_hi"])
+        mean_work = float(np.mean([m * (r * n - r * (r - 1) / 2.0) for m, n, r, p in specs]))
+
+        def item():
+            m, n, r, p = specs[int(rng.integers(0, len(specs)))]
+            A = (workloads.rank_deficient_modp(m, n, r, p, rng) if r < min(m, n)
+                 else rng.integers(0, p, size=(m, n), dtype=np.uint64))
+            return (lambda: oracle.rref_modp(A, p)), m * (r * n - r * (r - 1) / 2.0)
+        what = "uneven batch matrices (m ~ U[64,2048])"
+    else:
+        degs = range(wl["d_lo"], wl["d_hi"] + 1)
+        sizes = {d: workloads.monomial_indices(10, d).shape[0] for d in degs}
+        mean_work = float(np.mean([(n + 16) * n * (n + 1) / 2.0 for n in sizes.values()]))
+
+        def item():
+            d = int(rng.integers(wl["d_lo"], min(wl["d_hi"], 4) + 1))  # sizes a CPU finishes in seconds
+            p = workloads.random_prime_below(2**31, rng)
+            bases, lind = workloads.serve_load_request(rng, d, p)
+            n = lind.shape[0]
+            return (lambda: oracle.rref_modp(oracle.load_modp(bases, lind, p), p)), (n + 16) * n * (n + 1) / 2.0
+        what = "load+RREF requests of degree 3..4 (monomial loader + RREF)"
+    for _ in range(min(args.warmup, 1)):
+        f, _w = item()
+        f()
+    vals, descs = [], []
+    for _ in range(args.steps):
+        done_w, t, cnt = 0.0, 0.0, 0
+        while t < args.ref_seconds:
+            f, w = item()
+            t0 = time.perf_counter()
+            f()
+            t += time.perf_counter() - t0
+            done_w += w
+            cnt += 1
+        vals.append(done_w / t / mean_work)
+        descs.append(cnt)
+    desc = (f"{int(np.mean(descs))} whole solves per step of {what}, ~{args.ref_seconds:.0f} s each; "
+            f"rate scaled by work to the workload's mean solve")
+    return float(np.mean(vals)), oracle.default_threads(), desc
+
+
 def run_reference(args, dist: Dist):
     if dist.rank != 0:
         return None
     wl = WORKLOADS[args.workload]
+    if wl.get("batch") or wl.get("serve"):
+        t0 = time.perf_counter()
+        value, threads, desc = _reference_sampled(args, wl)
+        return {
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded, same generators as the GPU arm)",
+            "config": {"workload": args.workload, "parallelism": "cpu (all host threads)"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "linac's CPU row_reduce / loader algorithms (C restatement, OpenMP over rows)",
+            "host_wall_s": time.perf_counter() - t0,
+        }
     m, n, p = wl["m"], wl["n"], wl["p"]
     import oracle
     oracle.build()
@@ -586,6 +655,150 @@ def run_batch(args, dist: Dist):
     return line
 
 
+def run_serve(args, dist: Dist):
+    """Served load+RREF stream through linac_gb300.serving.Server (public API,
+    host inputs, results copied back to the host) against the plain path: one
+    cuda_load_matrix + one cuda_row_reduce call per request."""
+    from linac_gb300 import _lib, cuda_row_reduce, workloads
+    from linac_gb300.matrix_loader import cuda_load_matrix
+    from linac_gb300.serving import Server
+
+    if dist.world > 1:
+        _lib.check(_lib.lib().lnc_set_device(dist.local_rank))
+    wl = WORKLOADS[args.workload]
+    rng = np.random.default_rng(4040 + dist.rank)
+    per_step = args.serve_requests or wl["per_step"]
+
+    def make(count):
+        out = []
+        for _ in range(count):
+            d = int(rng.integers(wl["d_lo"], wl["d_hi"] + 1))
+            p = workloads.random_prime_below(2**31, rng)
+            bases, lind = workloads.serve_load_request(rng, d, p)
+            out.append((d, p, bases, lind))
+        return out
+
+    def work_of(req):  # W = sum_k m (n - c_k); full column rank: pivots 0..n-1
+        m, n = req[2].shape[0], req[3].shape[0]
+        return float(m) * (n * (n + 1) / 2.0)
+
+    def run_phase(srv, reqs, rate):
+        """Submit with Poisson arrivals at `rate` (inf: all at once); wait for all."""
+        gaps = rng.exponential(1.0 / rate, size=len(reqs)) if np.isfinite(rate) else np.zeros(len(reqs))
+        tickets = []
+        t0 = time.perf_counter()
+        due = t0
+        for (d, p, bases, lind), g in zip(reqs, gaps):
+            due += g
+            now = time.perf_counter()
+            if due > now:
+                time.sleep(due - now)
+            tickets.append(srv.submit_load(bases, lind, p))
+        ranks = []
+        for t in tickets:
+            _, piv, rank = t.result(copy=False)
+            ranks.append((rank, piv[:1], piv[-1:]))
+            t.release()
+        return time.perf_counter() - t0, ranks
+
+    srv = Server(max_inflight=args.serve_inflight)
+    for _ in range(args.warmup):
+        run_phase(srv, make(per_step), float("inf"))
+    srv.reset_stats()
+    reqs = [make(per_step) for _ in range(args.steps)]
+    dist.barrier()
+    launches0 = _lib.launch_count()
+    step_s, ok = [], True
+    with ClockSampler(dist.local_rank if dist.world > 1 else 0) as clk:
+        for batch in reqs:
+            dt, ranks = run_phase(srv, batch, args.serve_rate)
+            step_s.append(dt)
+            for (d, p, bases, lind), (rank, first, last) in zip(batch, ranks):
+                n = lind.shape[0]
+                ok = ok and rank == n and first == [0] and last == [n - 1]
+    launches = _lib.launch_count() - launches0
+    st_sat = srv.stats()
+    total_s = dist.max(sum(step_s))
+    n_req = dist.sum(float(per_step * args.steps))
+    value = n_req / total_s
+    work = sum(work_of(r) for b in reqs for r in b)
+    # ---- latency under load: Poisson arrivals at 70% of the measured throughput
+    srv.reset_stats()
+    lat_reqs = make(max(2 * per_step, 32))
+    run_phase(srv, lat_reqs, 0.7 * value / dist.world)
+    st_lat = srv.stats()
+    # ---- plain path on two requests of every degree; served results must match it bit for bit
+    plain_t, exact = {}, True
+    by_d = {}
+    for r in (x for b in reqs for x in b):
+        by_d.setdefault(r[0], []).append(r)
+    cuda_row_reduce(cuda_load_matrix(*reqs[0][0][2:4], field_characteristic=reqs[0][0][1]), reqs[0][0][1])
+    for d, rs in sorted(by_d.items()):
+        ts = []
+        for (dd, p, bases, lind) in rs[:2]:
+            t0 = time.perf_counter()
+            A = cuda_load_matrix(bases, lind, (bases.shape[0], lind.shape[0]), field_characteristic=p)
+            R_plain, piv_plain = cuda_row_reduce(A, field_characteristic=p, return_pivots=True)
+            ts.append(time.perf_counter() - t0)
+            t = srv.submit_load(bases, lind, p)
+            R, piv, rank = t.result(copy=False)
+            exact = exact and bool(np.array_equal(R, R_plain)) and piv == piv_plain
+            t.release()
+        plain_t[d] = float(np.mean(ts))
+    plain_s = sum(plain_t[r[0]] for b in reqs for r in b)
+    plain_value = per_step * args.steps / plain_s
+    srv.close()
+    peaks = measured_peaks()
+    mean_s = sum(step_s) / len(step_s)
+    h2d = sum(r[2].nbytes + r[3].nbytes for b in reqs for r in b) / len(reqs)
+    d2h = sum(4 * r[2].shape[0] * r[3].shape[0] + 8 * min(r[2].shape[0], r[3].shape[0]) for b in reqs for r in b) \
+        / len(reqs)
+    mix = {int(d): sum(1 for b in reqs for r in b if r[0] == d) for d in sorted(by_d)}
+    return {
+        "metric": METRIC,
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * mean_s,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32",
+        "data": "synthetic (seeded points, prefactors and primes; monomial ansatz d ~ U{3..8}, 10 variables)",
+        "config": {"workload": "served load+RREF stream: Poisson arrivals, random prime < 2^31, all monomials "
+                               "of degree <= d in 10 variables (<= 8000 columns), rows = columns + 16",
+                   "requests_per_step": per_step, "degree_mix": mix, "max_inflight": args.serve_inflight,
+                   "arrival_rate_per_s": args.serve_rate if np.isfinite(args.serve_rate) else "all at once",
+                   "l2": "each request's matrix (up to 256 MB) is written by the loader and reduced in HBM"},
+        "latency_ms": {"p50": st_lat["p50_ms"], "p99": st_lat["p99_ms"], "mean": st_lat["mean_ms"],
+                       "max": st_lat["max_ms"], "arrival_rate_per_s": 0.7 * value / dist.world,
+                       "requests": int(st_lat["completed"]),
+                       "note": "submit -> result on the host, Poisson arrivals at 70% of the measured throughput"},
+        "latency_ms_saturated": {"p50": st_sat["p50_ms"], "p99": st_sat["p99_ms"]},
+        "bit_exact": bool(exact and ok),
+        "redone_exhaustively": int(st_sat["redone"] + st_lat["redone"]),
+        "peak_device_bytes": int(st_sat["peak_bytes"]),
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "call": "linac_gb300.serving.Server.submit_load (host inputs, results on the host)",
+                "note": "the served path is end-to-end by construction: value is this measurement"},
+        "plain": {"value": plain_value, "unit": "solves/s",
+                  "call": "cuda_load_matrix + cuda_row_reduce per request (host arrays)",
+                  "seconds_per_request_by_degree": plain_t},
+        "served_vs_plain": value / plain_value,
+        "gpu_launches": launches,
+        "work_field_macs_per_step": work / len(reqs),
+        "roofline": {"bound": "tensor", "kernel": "limb GEMMs + candidate panels + loader (whole served run)",
+                     "achieved": 32.0 * work / sum(step_s) / 1e12, "peak": peaks["bf16_tflops_sustained"],
+                     "unit": "TFLOP/s",
+                     "frac": 32.0 * work / sum(step_s) / 1e12 / peaks["bf16_tflops_sustained"],
+                     "traffic": None, "peak_source": f"{peaks['source']} bf16 sustained",
+                     "note": "wall time of the served run incl. host copies; 2*4*4 bf16 flops per field multiply-add"},
+        "clocks": clk.summary(),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -601,6 +814,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="batched workloads: skip the autotuner")
     ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--serve-requests", type=int, default=0, help="served workload: requests per step")
+    ap.add_argument("--serve-inflight", type=int, default=16, help="served workload: requests in flight")
+    ap.add_argument("--serve-rate", type=float, default=float("inf"),
+                    help="served workload: Poisson arrival rate of the timed steps (default: all at once)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     dist = Dist()
@@ -614,6 +831,8 @@ def main():
             (_lib.LNC_FLAG_ROBUST_PANEL if args.robust_panel else 0)
         if WORKLOADS[args.workload].get("batch"):
             line = run_batch(args, dist)
+        elif WORKLOADS[args.workload].get("serve"):
+            line = run_serve(args, dist)
         else:
             line = run_ours(args, dist)
     if dist.rank == 0 and line is not None:

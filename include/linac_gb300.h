@@ -45,6 +45,12 @@ extern "C" {
 #define LNC_FLAG_NO_SCALING 1   /* float path: skip the row pre-scaling     */
 #define LNC_FLAG_SIMT_TRAILING 2 /* force the SIMT trailing update (tests)  */
 #define LNC_FLAG_ROBUST_PANEL 4  /* F_p: always use the exhaustive grid-wide panel */
+/* F_p, 32-bit: do not redo a candidate panel that missed a pivot in place (no
+ * grid-wide panel launch per panel, so concurrent solves on other streams are
+ * never held up).  A miss is reported through dev_rank = -1 instead (the
+ * outputs are then invalid and the caller redoes the solve with
+ * LNC_FLAG_ROBUST_PANEL); a device-side timeout through dev_rank = -2.       */
+#define LNC_FLAG_DEFER_FALLBACK 8
 
 /* ---- library / device ---------------------------------------------------- */
 /* Version string of the library. */
@@ -199,6 +205,76 @@ int lnc_load_matrix_device(int dtype, int64_t n_rows, int64_t n_cols, int64_t ba
                            int64_t degree, uint64_t p, const void* dev_bases,
                            const uint32_t* dev_lindices, void* dev_out, int64_t ld_out,
                            void* stream);
+
+/* ---- serving loop ------------------------------------------------------------ */
+/*
+ * A server owns a scheduler thread and a set of CUDA streams ("slots").
+ * Requests (an RREF of a host matrix, or a monomial load followed by the RREF
+ * of the loaded matrix) are queued by lnc_serve_submit and admitted while a
+ * slot is free and their device footprint (lnc_serve_request_bytes) fits the
+ * memory budget; an admitted request's matrix stays resident on the device
+ * from its load to its result copy, and the requests in flight run
+ * concurrently on their streams.  Requests that arrive while others run are
+ * admitted as slots and memory free up (continuous batching; later requests
+ * may pass a queued one that does not fit yet, a bounded number of times).
+ * F_p solves run with LNC_FLAG_DEFER_FALLBACK; a solve whose candidate panels
+ * missed a pivot is redone with LNC_FLAG_ROBUST_PANEL before it completes.
+ *
+ * Host buffers must stay valid until the request completes; page-locked
+ * buffers (lnc_malloc_host) let the copies overlap, pageable ones make the
+ * scheduler wait for each copy.
+ *
+ * No reference counterpart: linac's callers make one synchronous
+ * cuda_row_reduce / load_matrices call per system
+ * (linac/pycuda_row_reduce.py:18-151, linac/pycuda_matrix_loader.py:127-230).
+ */
+#define LNC_SERVE_RREF 1      /* RREF of host_in (m x n, ld_in)                       */
+#define LNC_SERVE_LOAD_RREF 2 /* load (bases, lindices) into an m x n matrix, then RREF */
+
+typedef struct lnc_serve_request {
+    int kind;                       /* LNC_SERVE_RREF or LNC_SERVE_LOAD_RREF          */
+    int dtype;                      /* LNC_U32 / LNC_U64 / LNC_F64 / LNC_C128          */
+    uint64_t p;                     /* prime (F_p dtypes)                              */
+    double tol;                     /* pivot threshold (float dtypes; <= 0: 1e-9)      */
+    int64_t m, n;                   /* matrix shape (load: points x monomials)         */
+    const void* host_in;            /* RREF: input matrix                              */
+    int64_t ld_in;
+    const void* host_bases;         /* load: m x basis_len values (dtype)              */
+    int64_t basis_len;
+    const uint32_t* host_lindices;  /* load: n x degree basis indices                  */
+    int64_t degree;
+    void* host_out;                 /* m x n result (ld_out)                           */
+    int64_t ld_out;
+    int64_t* host_pivot_cols;       /* min(m, n) entries (first rank valid) or NULL    */
+    int64_t* host_rank;             /* or NULL                                         */
+    int flags;                      /* LNC_FLAG_* for the solve                        */
+} lnc_serve_request;
+
+typedef struct lnc_serve_stats {
+    int64_t submitted, completed, failed, redone;
+    int64_t queued, inflight;
+    int64_t bytes_in_use, peak_bytes, budget_bytes;
+    double p50_ms, p99_ms, mean_ms, max_ms; /* submit -> result on the host, completed requests */
+} lnc_serve_stats;
+
+/* budget_bytes <= 0: 90% of the device memory free at creation; max_inflight <= 0: 16 */
+int lnc_server_create(int64_t budget_bytes, int max_inflight, void** server);
+/* cancels queued requests (LNC_ERR_INVALID), waits for those in flight */
+int lnc_server_destroy(void* server);
+/* device bytes the request holds while in flight (its admission size) */
+int64_t lnc_serve_request_bytes(const lnc_serve_request* req);
+/* LNC_ERR_ADMISSION when the request alone exceeds the budget */
+int lnc_serve_submit(void* server, const lnc_serve_request* req, int64_t* ticket);
+/* done = 1 once the results are in the host buffers; status = the request's LNC_* code */
+int lnc_serve_poll(void* server, int64_t ticket, int* done, int* status);
+/* LNC_OK when the request completed within timeout_s (< 0: no limit), else LNC_ERR_TIMEOUT */
+int lnc_serve_wait(void* server, int64_t ticket, double timeout_s, int* status);
+/* queue_ms: submit -> admission; total_ms: submit -> results on the host */
+int lnc_serve_latency(void* server, int64_t ticket, double* queue_ms, double* total_ms);
+/* forget a completed ticket */
+int lnc_serve_release(void* server, int64_t ticket);
+int lnc_serve_stats_read(void* server, lnc_serve_stats* out);
+int lnc_serve_stats_reset(void* server);
 
 #ifdef __cplusplus
 }

@@ -433,6 +433,12 @@ __global__ void publish_status_kernel(const int* err, int* status) {
     if (*err != 0) atomicExch(status, *err);
 }
 
+// deferred-fallback solves: the rank output carries the outcome
+__global__ void publish_deferred_kernel(const int* err, const int* missed_any, int64_t* dev_rank) {
+    if (*err != 0) *dev_rank = -2;
+    else if (missed_any && *missed_any) *dev_rank = -1;
+}
+
 // ----------------------------------------------------------------------------
 // host driver
 // ----------------------------------------------------------------------------
@@ -649,6 +655,8 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
     };
 
     bool fast = false;
+    const bool defer = (flags & LNC_FLAG_DEFER_FALLBACK) != 0;
+    int* defer_missed = nullptr;
     if constexpr (F::kDtype == 1) {
         fast = !(flags & (LNC_FLAG_SIMT_TRAILING | LNC_FLAG_ROBUST_PANEL)) && pl.b == kMaxPanel &&
                trailing_tc_u32_available();
@@ -665,7 +673,9 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
             int32_t* cand_n = (int32_t*)fscal;
             int32_t* next_row = (int32_t*)(fscal + 4);
             int* missed = (int*)(fscal + 8);
+            int* missed_any = (int*)(fscal + 12);  // sticky miss flag of a deferred-fallback solve
             uint32_t* pivmask = (uint32_t*)(fscal + 16);
+            defer_missed = missed_any;
             int32_t* panel_cols = (int32_t*)takef(sizeof(int32_t) * kMaxPanel);
             int32_t* panel_mark = (int32_t*)takef(sizeof(int32_t) * (size_t)m);
             int32_t* col_row = (int32_t*)takef(sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1));
@@ -723,8 +733,9 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
                 if (!rc) rc = tc_split_e(E, kMaxPanel, kMaxPanel, m, f.p, panel_k, EL, s);
                 if (!rc) rc = tc_gather_split_b(A + j0, lda, n - j0, panel_rows, panel_k, f.p, BS, true, s);
                 if (!rc) rc = tc_limb_gemm(f, A + j0, lda, m, n - j0, panel_k, false, EL, BS, n, err, status, s);
-                if (!rc) rc = launch_check_missed(A, lda, m, j0, bw, row_used, pivmask, missed, s);
+                if (!rc) rc = launch_check_missed(A, lda, m, j0, bw, row_used, pivmask, defer ? missed_any : missed, s);
                 if (rc) return rc;
+                if (defer) continue;
                 // redo the panel exhaustively when the candidate block missed a pivot
                 PanelArgs<F> pa = make_panel_args(j0, bw, j1 < n, missed);
                 rc = launch_panel(pa);
@@ -774,6 +785,10 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
     }
     publish_status_kernel<<<1, 1, 0, s>>>(err, status);
     LNC_CHECK_LAUNCH("publish_status_kernel");
+    if (defer && dev_rank) {
+        publish_deferred_kernel<<<1, 1, 0, s>>>(err, defer_missed, dev_rank);
+        LNC_CHECK_LAUNCH("publish_deferred_kernel");
+    }
     return LNC_OK;
 }
 
@@ -847,6 +862,18 @@ static int rref_device_typed(const F& f, void* work, int64_t ldw, void* out, int
     }
     cudaFreeAsync(scratch, s);
     return rc;
+}
+
+// device scratch one (out-of-place) solve allocates, 0 when the shape is not supported
+size_t rref_device_scratch(int dtype, int64_t m, int64_t n) {
+    RrefPlan pl;
+    switch (dtype) {
+        case LNC_U32: return plan_rref<FieldU32>(m, n, &pl) ? 0 : rref_scratch_bytes<FieldU32>(m, n, pl);
+        case LNC_U64: return plan_rref<FieldU64>(m, n, &pl) ? 0 : rref_scratch_bytes<FieldU64>(m, n, pl);
+        case LNC_F64: return plan_rref<FieldF64>(m, n, &pl) ? 0 : rref_scratch_bytes<FieldF64>(m, n, pl);
+        case LNC_C128: return plan_rref<FieldC128>(m, n, &pl) ? 0 : rref_scratch_bytes<FieldC128>(m, n, pl);
+        default: return 0;
+    }
 }
 
 int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* work,

@@ -217,5 +217,6 @@ int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol
                          int64_t ldw, void* out, int64_t ldo, int64_t* dev_piv, int64_t* dev_rank,
                          cudaStream_t s, int flags);
 int rref_read_and_clear_status(int* status);
+size_t rref_device_scratch(int dtype, int64_t m, int64_t n);
 
 }  // namespace lnc

@@ -15,12 +15,20 @@ same matrices on every machine.
   prime per matrix from the 64 largest primes below 2^31.
 * ``haar_orthogonal`` / ``conditioned_matrix`` -- U diag(s) V^T test matrices
   with log-spaced singular values for the float / complex path.
+* ``serve_load_request(rng, d, p)`` -- one served load+RREF request: all
+  monomials of total degree <= d in 10 variables (truncated to 8000), rows =
+  columns + 16 points uniform in F_p^10 with non-zero uniform prefactors, as
+  loader inputs (bases = [1, x_1..x_10, prefactor] per point, lindices = the
+  monomial's d basis columns + the prefactor column).
 """
 from __future__ import annotations
 
+import itertools
+from functools import lru_cache
+
 import numpy as np
 
-from .primes import largest_primes_below
+from .primes import is_prime, largest_primes_below
 
 P31 = 2**31 - 1
 P61 = 2**61 - 1
@@ -102,3 +110,40 @@ def conditioned_matrix(n: int, rng: np.random.Generator, cond: float = 1e6,
     V = haar_orthogonal(n, rng, complex_)
     s = np.logspace(0.0, np.log10(cond), n)
     return (U * s[None, :]) @ V.conj().T
+
+
+def random_prime_below(bound: int, rng: np.random.Generator, lo: int | None = None) -> int:
+    """A prime drawn uniformly-ish from [lo, bound) (default lo = bound / 2)."""
+    lo = bound // 2 if lo is None else lo
+    while True:
+        c = int(rng.integers(lo, bound)) | 1
+        if c < bound and is_prime(c):
+            return c
+
+
+@lru_cache(maxsize=16)
+def monomial_indices(n_vars: int, d: int, max_cols: int = 8000) -> np.ndarray:
+    """Basis columns of every monomial of total degree <= d in n_vars variables
+    (column 0 is the constant 1, column v the variable v): one row of d indices
+    per monomial, multisets in lexicographic order (so a truncation keeps the
+    lower degrees first), at most max_cols rows."""
+    rows = list(itertools.islice(itertools.combinations_with_replacement(range(n_vars + 1), d), max_cols))
+    out = np.array(rows, dtype=np.uint32).reshape(len(rows), d)
+    out.flags.writeable = False
+    return out
+
+
+def serve_load_request(rng: np.random.Generator, d: int, p: int, n_vars: int = 10, max_cols: int = 8000,
+                       extra_rows: int = 16):
+    """(bases, lindices) of one load+RREF request (see module docstring)."""
+    mono = monomial_indices(n_vars, d, max_cols)
+    n_cols = mono.shape[0]
+    n_rows = n_cols + extra_rows
+    bases = np.empty((n_rows, n_vars + 2), dtype=np.uint32)
+    bases[:, 0] = 1
+    bases[:, 1:n_vars + 1] = rng.integers(0, p, size=(n_rows, n_vars), dtype=np.uint64)
+    bases[:, n_vars + 1] = rng.integers(1, p, size=n_rows, dtype=np.uint64)
+    lind = np.empty((n_cols, d + 1), dtype=np.uint32)
+    lind[:, :d] = mono
+    lind[:, d] = n_vars + 1
+    return bases, lind

@@ -55,6 +55,11 @@ WORKLOADS = {
     # a prime per matrix from the 64 largest primes below 2^31, built as B.C on the device
     "batch4096": dict(count=4096, m_lo=64, m_hi=2048, dtype="u32", batch=True),
     "batch512": dict(count=512, m_lo=64, m_hi=2048, dtype="u32", batch=True),
+    # float / complex: U diag(s) V^H (Haar U, V; s log-spaced over [1, 1e6]) with a 16-column
+    # right-hand side; mixed precision (fixed-point tensor-core updates + FP64 refinement)
+    "rref_f64_5000": dict(n=5000, rhs=16, cplx=False, dtype="f64", float=True),
+    "rref_c128_5000": dict(n=5000, rhs=16, cplx=True, dtype="c128", float=True),
+    "rref_f64_2000": dict(n=2000, rhs=16, cplx=False, dtype="f64", float=True),
     # served load+RREF stream: Poisson arrivals, a random prime below 2^31 per request, all
     # monomials of degree <= d (d ~ U{3..8}) in 10 variables truncated to 8000 columns,
     # rows = columns + 16 points uniform in F_p^10, non-zero uniform prefactors
@@ -462,6 +467,32 @@ def run_reference(args, dist: Dist):
     if dist.rank != 0:
         return None
     wl = WORKLOADS[args.workload]
+    if wl.get("float"):
+        import oracle
+        from linac_gb300 import workloads
+        oracle.build()
+        n0 = min(wl["n"], 1200)
+        rng = np.random.default_rng(5000)
+        A = workloads.conditioned_matrix(n0, rng, cond=1e6, complex_=wl["cplx"])
+        Bq = rng.standard_normal((n0, wl["rhs"])) + (1j * rng.standard_normal((n0, wl["rhs"])) if wl["cplx"] else 0)
+        M = np.hstack([A, Bq])
+        f = oracle.rref_c128 if wl["cplx"] else oracle.rref_f64
+        ts = []
+        for _ in range(max(args.steps, 1)):
+            t0 = time.perf_counter()
+            f(M)
+            ts.append(time.perf_counter() - t0)
+        scale = (wl["n"] / n0) ** 3
+        value = 1.0 / (float(np.mean(ts)) * scale)
+        desc = f"whole {n0}x{n0 + wl['rhs']} solves by the oracle, extrapolated by n^3 to n = {wl['n']}"
+        return {
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "parallelism": "cpu (one thread)"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
     if wl.get("batch") or wl.get("serve"):
         t0 = time.perf_counter()
         value, threads, desc = _reference_sampled(args, wl)
@@ -655,6 +686,122 @@ def run_batch(args, dist: Dist):
     return line
 
 
+def run_float(args, dist: Dist):
+    """Mixed-precision float / complex RREF of [A | B] (A = U diag(s) V^H,
+    cond 1e6) against the FP64 path on the same device, with the max-norm
+    error of both against the FP64 oracle and against a refined solution."""
+    from linac_gb300 import _lib, cuda_row_reduce, pinned_empty, workloads
+    import oracle
+
+    if dist.world > 1:
+        _lib.check(_lib.lib().lnc_set_device(dist.local_rank))
+    wl = WORKLOADS[args.workload]
+    n, q, cplx = wl["n"], wl["rhs"], wl["cplx"]
+    dt = np.complex128 if cplx else np.float64
+    code = _lib.LNC_C128 if cplx else _lib.LNC_F64
+    rng = np.random.default_rng(5000 + dist.rank)
+    A = workloads.conditioned_matrix(n, rng, cond=1e6, complex_=cplx)
+    Bq = rng.standard_normal((n, q)) + (1j * rng.standard_normal((n, q)) if cplx else 0)
+    host_in = pinned_empty((n, n + q), dt)
+    host_in[:] = np.hstack([A, Bq])
+    host_out = pinned_empty((n, n + q), dt)
+    m, cols = n, n + q
+    L = _lib.lib()
+    nbytes = host_in.nbytes
+    d_src, d_work, d_out = _lib.DeviceBuffer(nbytes), _lib.DeviceBuffer(nbytes), _lib.DeviceBuffer(nbytes)
+    d_piv, d_rank = _lib.DeviceBuffer(8 * m), _lib.DeviceBuffer(8)
+    stream = _lib.Stream()
+    d_src.upload(host_in, stream.handle)
+
+    def solve(flags):
+        _lib.check(L.lnc_memcpy_d2d(d_work.ptr, d_src.ptr, nbytes, stream.handle))
+        _lib.check(L.lnc_rref_device(code, m, cols, 0, 1e-9, d_work.ptr, cols, d_out.ptr, cols, d_piv.ptr,
+                                     d_rank.ptr, stream.handle, flags))
+
+    def timed(flags, steps):
+        for _ in range(args.warmup):
+            solve(flags)
+        stream.synchronize()
+        dist.barrier()
+        ev = [(_lib.Event(), _lib.Event()) for _ in range(steps)]
+        l0 = _lib.launch_count()
+        for i in range(steps):
+            ev[i][0].record(stream.handle)
+            solve(flags)
+            ev[i][1].record(stream.handle)
+        stream.synchronize()
+        return [a.elapsed_ms(b) for a, b in ev], _lib.launch_count() - l0
+
+    _lib.kernel_timing(True)
+    with ClockSampler(dist.local_rank if dist.world > 1 else 0) as clk:
+        lat, launches = timed(_lib.LNC_FLAG_MIXED, args.steps)
+    kt = {name: _lib.kernel_timing_read(kc) for name, kc in (("panel", _lib.KC_PANEL), ("trailing", _lib.KC_TRAILING))}
+    kt_work = _lib.kernel_timing_work(_lib.KC_TRAILING)
+    _lib.kernel_timing(False)
+    rep = _lib.mixed_report()
+    d_out.download(host_out, stream.handle)
+    R_mixed = np.array(host_out)
+    lat_fp64, _ = timed(0, max(1, min(args.steps, 2)))
+    d_out.download(host_out, stream.handle)
+    R_fp64 = np.array(host_out)
+    t_max = dist.max(sum(lat) / 1000.0)
+    value = dist.sum(float(args.steps)) / t_max
+    # ---- end-to-end through cuda_row_reduce (pinned host arrays)
+    cuda_row_reduce(host_in, 0, out=host_out, mixed=True)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    for _ in range(e2e_steps):
+        cuda_row_reduce(host_in, 0, out=host_out, mixed=True)
+    t_e2e = dist.max(time.perf_counter() - t0)
+    # ---- errors (untimed): vs a refined solution and vs the FP64 oracle
+    X = np.linalg.solve(A, Bq)
+    Al = A.astype(np.clongdouble if cplx else np.longdouble)
+    for _ in range(3):
+        X = X + np.linalg.solve(A, (Bq - (Al @ X.astype(Al.dtype))).astype(dt))
+
+    def rel(Y, Z):
+        return float(np.abs(Y - Z).max() / np.abs(Z).max())
+    err = {"mixed_vs_refined_solution": rel(R_mixed[:, n:], X), "fp64_path_vs_refined_solution": rel(R_fp64[:, n:], X),
+           "mixed_vs_fp64_path": rel(R_mixed, R_fp64), "pivot_block_is_identity": bool(np.array_equal(R_mixed[:, :n], np.eye(n)))}
+    cpu = None
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        R_o, piv_o, rank_o = (oracle.rref_c128 if cplx else oracle.rref_f64)(host_in)
+        t_o = time.perf_counter() - t0
+        err["mixed_vs_fp64_oracle"] = rel(R_mixed, R_o)
+        err["oracle_vs_refined_solution"] = rel(R_o[:, n:], X)
+        cpu = {"value": 1.0 / t_o, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"one whole {m}x{cols} {'complex128' if cplx else 'float64'} RREF by the oracle "
+                         "(linac's CPU row_reduce, pivoting=1, scaling=True, threshold 1e-9)"}
+    peaks = measured_peaks()
+    tr_cnt, tr_ms = kt["trailing"]
+    # kt_work: real multiply-adds of the trailing updates (4 per complex one); 32 bf16 flops each
+    tr_ach = 32.0 * kt_work / (tr_ms / 1e3) / 1e12 if tr_ms > 0 else None
+    return {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sum(lat) / len(lat), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128" if cplx else "f64",
+        "data": "synthetic (Haar U, V from QR of Gaussians, s log-spaced over [1, 1e6]; Gaussian RHS; seeded)",
+        "config": {"workload": f"{'complex128' if cplx else 'float64'} RREF of [A | B], A {n}x{n} cond 1e6, "
+                               f"B {n}x{q}", "precision": "mixed: 31-bit fixed-point tensor-core updates, "
+                               "FP64 panels and refinement", "l2": f"input {nbytes / 1e6:.0f} MB > L2"},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "fp64_path_ms": float(np.mean(lat_fp64)), "mixed_speedup_vs_fp64_path": float(np.mean(lat_fp64) / np.mean(lat)),
+        "refinement": rep, "errors_max_norm_relative": err,
+        "kernel_ms": {k: {"launches": c, "total_ms": t} for k, (c, t) in kt.items()},
+        "e2e": {"value": dist.sum(float(e2e_steps)) / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes + 8 * m, "call": "cuda_row_reduce(..., mixed=True), pinned arrays"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "tensor", "kernel": "limb_gemm_kernel (fixed-point epilogue)", "achieved": tr_ach,
+                     "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                     "frac": (tr_ach / peaks["bf16_tflops_sustained"]) if tr_ach else None, "traffic": None,
+                     "peak_source": f"{peaks['source']} bf16 sustained",
+                     "note": "16 BF16 digit products (32 flops) per real multiply-add of the trailing updates"},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+
+
 def run_serve(args, dist: Dist):
     """Served load+RREF stream through linac_gb300.serving.Server (public API,
     host inputs, results copied back to the host) against the plain path: one
@@ -833,6 +980,8 @@ def main():
             line = run_batch(args, dist)
         elif WORKLOADS[args.workload].get("serve"):
             line = run_serve(args, dist)
+        elif WORKLOADS[args.workload].get("float"):
+            line = run_float(args, dist)
         else:
             line = run_ours(args, dist)
     if dist.rank == 0 and line is not None:

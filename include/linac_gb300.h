@@ -51,6 +51,16 @@ extern "C" {
  * outputs are then invalid and the caller redoes the solve with
  * LNC_FLAG_ROBUST_PANEL); a device-side timeout through dev_rank = -2.       */
 #define LNC_FLAG_DEFER_FALLBACK 8
+/* float64 / complex128: mixed precision.  Trailing updates run on the tensor
+ * cores as exact products of 31-bit fixed-point operands (BF16 digits, FP32
+ * accumulation); panels, pivot choice and threshold stay FP64; the non-pivot
+ * columns of the result are then refined in FP64 (residual of the row-scaled
+ * input, correction through the stored panel transforms) until the
+ * correction stops shrinking.  When a pivot candidate's magnitude falls
+ * between 10^-3 and 10^5 times the threshold (a rank decision the
+ * reduced-precision updates could change) the solve is redone in FP64.  Synchronises the
+ * stream; lnc_mixed_report describes the last such solve of the thread.     */
+#define LNC_FLAG_MIXED 16
 
 /* ---- library / device ---------------------------------------------------- */
 /* Version string of the library. */
@@ -188,6 +198,12 @@ int lnc_fill_uniform_modp(void* dev_ptr, int64_t count, uint64_t p, uint64_t see
  * used to build rank-deficient inputs B.C on the device. */
 int lnc_matmul_modp_device(int dtype, int64_t m, int64_t k, int64_t n, uint64_t p, const void* A, int64_t lda,
                            const void* B, int64_t ldb, void* C, int64_t ldc, void* stream);
+
+/* Outcome of the calling thread's last LNC_FLAG_MIXED solve: refinement
+ * iterations, the last correction's max-norm relative to the refined
+ * entries, and whether the solve was redone in FP64.  No reference
+ * counterpart (linac's float path is FP64 only, linac/row_reduce.cu:55-270). */
+int lnc_mixed_report(int* iterations, double* last_correction, int* redone_fp64);
 
 /* ---- monomial loader --------------------------------------------------------- */
 /*

@@ -33,6 +33,8 @@ LNC_FLAG_NONE = 0
 LNC_FLAG_NO_SCALING = 1
 LNC_FLAG_SIMT_TRAILING = 2
 LNC_FLAG_ROBUST_PANEL = 4
+LNC_FLAG_DEFER_FALLBACK = 8
+LNC_FLAG_MIXED = 16
 
 KC_PANEL, KC_TRAILING, KC_LOADER, KC_GATHER, KC_BATCH = 0, 1, 2, 3, 4
 
@@ -96,6 +98,7 @@ _SIGNATURES = {
     "lnc_load_matrix_host": ([_int, _i64, _i64, _i64, _i64, _u64, _vp, _vp, _vp], _int),
     "lnc_load_matrix_device": ([_int, _i64, _i64, _i64, _i64, _u64, _vp, _vp, _vp, _i64, _vp], _int),
     "lnc_fill_uniform_modp": ([_vp, _i64, _u64, _u64, _int, _vp], _int),
+    "lnc_mixed_report": ([_vp, _vp, _vp], _int),
     "lnc_matmul_modp_device": ([_int, _i64, _i64, _i64, _u64, _vp, _i64, _vp, _i64, _vp, _i64, _vp], _int),
 }
 
@@ -310,3 +313,10 @@ def device_info():
 
 def device_status():
     check(lib().lnc_device_status(), "device status")
+
+
+def mixed_report() -> dict:
+    """Outcome of this thread's last mixed-precision float solve."""
+    it, corr, redone = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_int(0)
+    check(lib().lnc_mixed_report(ctypes.byref(it), ctypes.byref(corr), ctypes.byref(redone)), "lnc_mixed_report")
+    return {"iterations": it.value, "last_correction": corr.value, "redone_fp64": bool(redone.value)}

@@ -202,8 +202,8 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
     J.off = M.off;
     J.err = err;
     J.status = status;
-    if (J.redc) tc::limb_cta<true>(J, &tmA, &tmB);
-    else tc::limb_cta<false>(J, &tmA, &tmB);
+    if (J.redc) tc::limb_cta<tc::EPI_REDC>(J, &tmA, &tmB);
+    else tc::limb_cta<tc::EPI_BARRETT>(J, &tmA, &tmB);
 }
 
 static __global__ void batch_check_kernel(const BatchMat* mats, const int* active, int step) {

@@ -310,6 +310,10 @@ int lnc_event_elapsed_ms(void* a, void* b, float* ms) {
     return LNC_OK;
 }
 
+int lnc_mixed_report(int* iterations, double* last_correction, int* redone_fp64) {
+    return mixed_report(iterations, last_correction, redone_fp64);
+}
+
 int lnc_device_status(void) {
     LNC_CUDA(cudaDeviceSynchronize());
     int st = 0;

@@ -24,6 +24,7 @@
 //
 // The RREF over a field is unique, so the pivot order does not change the
 // F_p result; it is bit-identical to linac's CPU row_reduce.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
@@ -226,6 +227,9 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_kernel(PanelArgs<F> a)
                 s_win_row = wr;
                 s_win_blk = wb;
                 s_win_ok = (wr != INT64_MAX) && f.is_pivot(wk);
+                if constexpr (F::kDtype >= 3) {
+                    if (a.uncertain && wr != INT64_MAX && wk > a.band_lo && wk <= a.band_hi) atomicExch(a.uncertain, 1);
+                }
             }
             __syncthreads();
         }
@@ -547,10 +551,26 @@ size_t rref_scratch_bytes(int64_t m, int64_t n, const RrefPlan& pl) {
     return s;
 }
 
+// Extra state of a mixed-precision float solve: the row-scaled input kept
+// for the refinement residuals, every panel's transform (E columns and pivot
+// rows, which define the elimination's product of transforms M), the
+// fixed-point update scratch and the uncertain-rank-decision flag.
+template <class T>
+struct MixedCtx {
+    T* As = nullptr;           // m x n
+    T* E_all = nullptr;        // m x ldE, panel q in columns [q b, q b + b)
+    int64_t ldE = 0;
+    int32_t* P_all = nullptr;  // pivot rows of panel q at [q b, q b + b)
+    int32_t* K_all = nullptr;  // pivots of panel q
+    void* fx = nullptr;
+    int* uncertain = nullptr;
+};
+
 template <class F>
 int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, typename F::T* out,
              int64_t ldo, int64_t* dev_piv, int64_t* dev_rank, cudaStream_t s, int flags,
-             void* scratch, size_t scratch_bytes, const RrefPlan& pl) {
+             void* scratch, size_t scratch_bytes, const RrefPlan& pl,
+             MixedCtx<typename F::T>* mx = nullptr) {
     using T = typename F::T;
     const int64_t kmax = std::min(m, n);
     // carve scratch
@@ -593,6 +613,9 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
                 row_scale_kernel<F><<<(unsigned)std::min<int64_t>(m, 65535), 256, 0, s>>>(f, A, lda, m, n);
                 LNC_CHECK_LAUNCH("row_scale_kernel");
             }
+            if (mx)
+                LNC_CUDA(cudaMemcpy2DAsync(mx->As, sizeof(T) * n, A, sizeof(T) * lda, sizeof(T) * n, m,
+                                           cudaMemcpyDeviceToDevice, s));
         }
     }
 
@@ -616,6 +639,7 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
     tctx.extra = extra;
     tctx.b = pl.b;
     tctx.force_simt = (flags & LNC_FLAG_SIMT_TRAILING) != 0;
+    if (mx) tctx.fx = mx->fx;
 
     auto make_panel_args = [&](int64_t j0, int bw, bool with_e, const int* run_if) {
         PanelArgs<F> pa;
@@ -758,7 +782,23 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
             const int bw = (int)std::min<int64_t>(pl.b, n - j0);
             const int64_t j1 = j0 + bw;
             const int64_t N = n - j1;
-            PanelArgs<F> pa = make_panel_args(j0, bw, N > 0, nullptr);
+            PanelArgs<F> pa = make_panel_args(j0, bw, N > 0 || mx != nullptr, nullptr);
+            if constexpr (F::kDtype >= 3) {
+                if (mx) {  // keep every panel's transform for the refinement
+                    const int64_t q = j0 / pl.b;
+                    pa.E = mx->E_all + q * pl.b;
+                    pa.ldE = mx->ldE;
+                    pa.panel_k = mx->K_all + q;
+                    pa.panel_rows = mx->P_all + q * pl.b;
+                    pa.uncertain = mx->uncertain;
+                    pa.band_lo = 1e-3 * f.tol;
+                    pa.band_hi = 1e5 * f.tol;  // well above the fixed-point updates' noise
+                    tctx.E = pa.E;
+                    tctx.ldE = pa.ldE;
+                    tctx.panel_k = pa.panel_k;
+                    tctx.panel_rows = pa.panel_rows;
+                }
+            }
             int rc = launch_panel(pa);
             if (rc) return rc;
             if (N > 0) {
@@ -864,6 +904,168 @@ static int rref_device_typed(const F& f, void* work, int64_t ldw, void* out, int
     return rc;
 }
 
+// ----------------------------------------------------------------------------
+// mixed-precision float solve: fixed-point tensor-core elimination, then FP64
+// refinement of the non-pivot columns (see trailing_fx.cu)
+// ----------------------------------------------------------------------------
+struct MixedReport {
+    int iterations = 0;
+    double last_correction = 0.0;
+    int redone = 0;
+};
+static thread_local MixedReport t_mixed;
+
+template <class F>
+static int rref_mixed_typed(const F& f, void* work, int64_t ldw, void* out, int64_t ldo, int64_t m, int64_t n,
+                            int64_t* dev_piv, int64_t* dev_rank, cudaStream_t s, int flags) {
+    using T = typename F::T;
+    constexpr bool CPLX = F::kDtype == LNC_C128;
+    t_mixed = MixedReport();
+    RrefPlan pl;
+    int rc = plan_rref<F>(m, n, &pl);
+    if (rc) return rc;
+    if (CPLX && pl.b > 64) {  // realified contraction depth 2b <= 128
+        pl.b = 64;
+        pl.smem = panel_smem_bytes<F>(pl.rows_per_cta, (int)std::min<int64_t>(pl.b, n));
+    }
+    if (flags & LNC_FLAG_NO_SCALING) { set_error("mixed precision needs the row scaling"); return LNC_ERR_INVALID; }
+    const int64_t panels = (n + pl.b - 1) / pl.b;
+    const int64_t kmax = std::min(m, n);
+    const size_t sb = rref_scratch_bytes<F>(m, n, pl);
+    const size_t as_b = align_up(sizeof(T) * (size_t)m * n, 256);
+    const size_t e_b = align_up(sizeof(T) * (size_t)m * panels * pl.b, 256);
+    const size_t p_b = align_up(sizeof(int32_t) * (size_t)panels * pl.b, 256);
+    const size_t k_b = align_up(sizeof(int32_t) * (size_t)panels, 256);
+    const size_t fx_b = align_up(trailing_fx_scratch(m, n, CPLX), 256);
+    const size_t out_b = align_up(sizeof(T) * (size_t)m * n, 256);  // out of place result
+    const size_t total = sb + as_b + e_b + p_b + k_b + fx_b + out_b + 256;
+    unsigned char* blk = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&blk, total, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("mixed-precision scratch of %zu bytes: %s", total, cudaGetErrorString(e));
+        return LNC_ERR_OOM;
+    }
+    unsigned char* q = blk + sb;
+    MixedCtx<T> mx;
+    mx.As = (T*)q; q += as_b;
+    mx.E_all = (T*)q; q += e_b;
+    mx.ldE = panels * pl.b;
+    mx.P_all = (int32_t*)q; q += p_b;
+    mx.K_all = (int32_t*)q; q += k_b;
+    mx.fx = q; q += fx_b;
+    T* R = (T*)q; q += out_b;
+    mx.uncertain = (int*)q;
+    auto fail = [&](int code) { cudaFreeAsync(blk, s); return code; };
+    LNC_CUDA(cudaMemsetAsync(mx.uncertain, 0, 256, s));
+    LNC_CUDA(cudaMemsetAsync(mx.K_all, 0, sizeof(int32_t) * panels, s));
+    const int run_flags = flags & ~(LNC_FLAG_MIXED | LNC_FLAG_DEFER_FALLBACK);
+    rc = rref_run<F>(f, (T*)work, m, n, ldw, R, n, nullptr, nullptr, s, run_flags, blk, sb, pl, &mx);
+    if (rc) return fail(rc);
+    // pivots of the mixed elimination (scratch layout of rref_run: row_used, piv_row, piv_col, scalars)
+    unsigned char* sp = blk;
+    sp += align_up((size_t)m, 256);
+    int32_t* piv_row = (int32_t*)sp;
+    sp += align_up(sizeof(int32_t) * (size_t)std::max<int64_t>(kmax, 1), 256);
+    int64_t* piv_col = (int64_t*)sp;
+    sp += align_up(sizeof(int64_t) * (size_t)std::max<int64_t>(kmax, 1), 256);
+    int64_t* rank_d = (int64_t*)sp;
+    int64_t rank = 0;
+    int unc = 0;
+    LNC_CUDA(cudaMemcpyAsync(&rank, rank_d, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    LNC_CUDA(cudaMemcpyAsync(&unc, mx.uncertain, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LNC_CUDA(cudaStreamSynchronize(s));
+    if (unc) {
+        // a rank decision within reach of the reduced precision: redo in FP64 from the scaled input
+        t_mixed.redone = 1;
+        LNC_CUDA(cudaMemcpy2DAsync(work, sizeof(T) * ldw, mx.As, sizeof(T) * n, sizeof(T) * n, m,
+                                   cudaMemcpyDeviceToDevice, s));
+        rc = rref_run<F>(f, (T*)work, m, n, ldw, R, n, nullptr, nullptr, s, run_flags | LNC_FLAG_NO_SCALING, blk,
+                         sb, pl);
+        if (rc) return fail(rc);
+        LNC_CUDA(cudaMemcpyAsync(&rank, rank_d, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        LNC_CUDA(cudaStreamSynchronize(s));
+    } else if (rank > 0 && rank < n) {
+        // ---- FP64 refinement of the non-pivot columns
+        const int qn = (int)(n - rank);
+        std::vector<int64_t> pc((size_t)rank);
+        LNC_CUDA(cudaMemcpy(pc.data(), piv_col, sizeof(int64_t) * rank, cudaMemcpyDeviceToHost));
+        std::vector<int32_t> colmap((size_t)n, -1), nc;
+        nc.reserve((size_t)qn);
+        for (int64_t t = 0; t < rank; ++t) colmap[(size_t)pc[(size_t)t]] = (int32_t)t;
+        for (int64_t c = 0; c < n; ++c)
+            if (colmap[(size_t)c] < 0) nc.push_back((int32_t)c);
+        const size_t z_b = align_up(sizeof(T) * (size_t)n * qn, 256);
+        const size_t r_b = align_up(sizeof(T) * (size_t)m * qn, 256);
+        const size_t g_b = align_up(sizeof(T) * (size_t)pl.b * qn, 256);
+        const size_t i_b = align_up(sizeof(int32_t) * (size_t)(n + qn), 256);
+        unsigned char* rb = nullptr;
+        e = cudaMallocAsync((void**)&rb, z_b + r_b + g_b + i_b + 256, s);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error("refinement scratch: %s", cudaGetErrorString(e));
+            return fail(LNC_ERR_OOM);
+        }
+        T* Z = (T*)rb;
+        T* Res = (T*)(rb + z_b);
+        T* Bg = (T*)(rb + z_b + r_b);
+        int32_t* d_colmap = (int32_t*)(rb + z_b + r_b + g_b);
+        int32_t* d_nc = d_colmap + n;
+        unsigned long long* stats = (unsigned long long*)(rb + z_b + r_b + g_b + i_b);
+        LNC_CUDA(cudaMemcpyAsync(d_colmap, colmap.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+        LNC_CUDA(cudaMemcpyAsync(d_nc, nc.data(), sizeof(int32_t) * qn, cudaMemcpyHostToDevice, s));
+        double prev = INFINITY;
+        for (int it = 0; it < 10 && !rc; ++it) {
+            rc = refine_build_z<T>(n, qn, d_colmap, d_nc, R, n, Z, s);
+            if (!rc) {
+                LNC_CUDA(cudaMemsetAsync(Res, 0, sizeof(T) * (size_t)m * qn, s));
+                rc = refine_narrow_gemm<T>(m, qn, n, nullptr, mx.As, n, Z, qn, Res, qn, s);
+            }
+            for (int64_t pq = 0; pq < panels && !rc; ++pq) {  // Res <- M Res, panel by panel
+                dim3 g((unsigned)std::max<int64_t>(1, std::min<int64_t>((qn + 255) / 256, 64)), (unsigned)pl.b);
+                gather_pivot_rows_kernel<F><<<g, 256, 0, s>>>(f, Res, qn, 0, qn, mx.P_all + pq * pl.b,
+                                                              mx.K_all + pq, Bg, qn);
+                LNC_CHECK_LAUNCH("gather_pivot_rows_kernel (refinement)");
+                rc = refine_narrow_gemm<T>(m, qn, pl.b, mx.K_all + pq, mx.E_all + pq * pl.b, mx.ldE, Bg, qn, Res, qn,
+                                           s);
+            }
+            if (rc) break;
+            LNC_CUDA(cudaMemsetAsync(stats, 0, 16, s));
+            rc = refine_apply<T>(rank, qn, piv_row, d_nc, Res, R, n, stats, s);
+            if (rc) break;
+            unsigned long long hs[2];
+            LNC_CUDA(cudaMemcpyAsync(hs, stats, 16, cudaMemcpyDeviceToHost, s));
+            LNC_CUDA(cudaStreamSynchronize(s));
+            double corr, ymax;
+            memcpy(&corr, &hs[0], 8);
+            memcpy(&ymax, &hs[1], 8);
+            t_mixed.iterations = it + 1;
+            t_mixed.last_correction = ymax > 0 ? corr / ymax : corr;
+            if (corr <= 4.0 * 1.1102230246251565e-16 * ymax || corr >= 0.5 * prev) break;
+            prev = corr;
+        }
+        cudaFreeAsync(rb, s);
+        if (rc) return fail(rc);
+    }
+    // outputs: the result (refined), pivots and rank
+    LNC_CUDA(cudaMemcpy2DAsync(out, sizeof(T) * ldo, R, sizeof(T) * n, sizeof(T) * n, m, cudaMemcpyDeviceToDevice,
+                               s));
+    if (dev_piv || dev_rank) {
+        copy_pivots_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((kmax + 255) / 256, 1024)), 256, 0,
+                             s>>>(piv_col, rank_d, kmax, dev_piv, dev_rank);
+        LNC_CHECK_LAUNCH("copy_pivots_kernel");
+    }
+    cudaFreeAsync(blk, s);
+    return LNC_OK;
+}
+
+int mixed_report(int* iterations, double* last_correction, int* redone) {
+    if (iterations) *iterations = t_mixed.iterations;
+    if (last_correction) *last_correction = t_mixed.last_correction;
+    if (redone) *redone = t_mixed.redone;
+    return LNC_OK;
+}
+
 // device scratch one (out-of-place) solve allocates, 0 when the shape is not supported
 size_t rref_device_scratch(int dtype, int64_t m, int64_t n) {
     RrefPlan pl;
@@ -882,8 +1084,14 @@ int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol
     switch (dtype) {
         case LNC_U32: return rref_device_typed(FieldU32::make(p), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
         case LNC_U64: return rref_device_typed(FieldU64::make(p), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
-        case LNC_F64: return rref_device_typed(FieldF64::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
-        case LNC_C128: return rref_device_typed(FieldC128::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        case LNC_F64:
+            if (flags & LNC_FLAG_MIXED)
+                return rref_mixed_typed(FieldF64::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+            return rref_device_typed(FieldF64::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+        case LNC_C128:
+            if (flags & LNC_FLAG_MIXED)
+                return rref_mixed_typed(FieldC128::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
+            return rref_device_typed(FieldC128::make(tol), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
         default: set_error("unknown dtype %d", dtype); return LNC_ERR_INVALID;
     }
 }
@@ -972,6 +1180,7 @@ extern "C" int lnc_rref_device_noalloc(int dtype, int64_t m, int64_t n, uint64_t
     using namespace lnc;
     int rc = validate_rref_args(dtype, m, n, p, ld_work);
     if (rc) return rc;
+    if (flags & LNC_FLAG_MIXED) { set_error("mixed precision allocates: not available without allocation"); return LNC_ERR_UNSUPPORTED; }
     if (ld_out < n) { set_error("output leading dimension %lld < n", (long long)ld_out); return LNC_ERR_INVALID; }
     if (m == 0 || n == 0) {
         set_error("the no-allocation RREF needs a non-empty matrix");

@@ -40,6 +40,11 @@ struct PanelArgs {
     GridBarrier bar;
     int rows_per_cta;
     const int* run_if;      // optional: the kernel does nothing unless *run_if != 0
+    // float path, mixed precision: set *uncertain when a column's best pivot
+    // candidate has magnitude in (band_lo, band_hi] (a rank decision the
+    // reduced-precision updates could have tipped)
+    int* uncertain = nullptr;
+    double band_lo = 0.0, band_hi = 0.0;
 };
 
 // Multiply-accumulate policy of the SIMT trailing update, per field.
@@ -137,6 +142,7 @@ struct TrailingCtx {
     int64_t j1 = 0, N = 0;             // trailing columns [j1, j1 + N)
     bool force_simt = false;
     bool predicated = false;           // runs only if the panel before it found pivots (fallback)
+    void* fx = nullptr;                // float path: fixed-point tensor-core update scratch (mixed precision)
 };
 
 template <class F>
@@ -205,10 +211,28 @@ inline size_t trailing_extra_scratch(int64_t m, int64_t n, const RrefPlan& pl) {
     return 0;
 }
 
+// Fixed-point tensor-core trailing update of the float path (trailing_fx.cu)
+template <class F>
+int trailing_update_fx(const TrailingCtx<F>& t, cudaStream_t s);
+size_t trailing_fx_scratch(int64_t m, int64_t n, bool cplx);
+// FP64 refinement kernels (trailing_fx.cu)
+template <class T>
+int refine_narrow_gemm(int64_t m, int q, int64_t K, const int32_t* k_ptr, const T* A, int64_t lda, const T* B,
+                       int64_t ldb, T* C, int64_t ldc, cudaStream_t s);
+template <class T>
+int refine_build_z(int64_t n, int q, const int32_t* colmap, const int32_t* Nc, const T* R, int64_t ldr, T* Z,
+                   cudaStream_t s);
+template <class T>
+int refine_apply(int64_t rank, int q, const int32_t* piv_row, const int32_t* Nc, const T* D, T* R, int64_t ldr,
+                 unsigned long long* stats, cudaStream_t s);
+
 template <class F>
 inline int trailing_update(const TrailingCtx<F>& t, cudaStream_t s) {
     if constexpr (F::kDtype == 1) {
         if (!t.force_simt && trailing_tc_u32_available()) return trailing_update_tc_u32(t, s);
+    }
+    if constexpr (F::kDtype == 3 || F::kDtype == 4) {
+        if (t.fx) return trailing_update_fx<F>(t, s);
     }
     return trailing_update_simt<F>(t, s);
 }
@@ -218,5 +242,6 @@ int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol
                          cudaStream_t s, int flags);
 int rref_read_and_clear_status(int* status);
 size_t rref_device_scratch(int dtype, int64_t m, int64_t n);
+int mixed_report(int* iterations, double* last_correction, int* redone);
 
 }  // namespace lnc

@@ -29,6 +29,10 @@ constexpr uint32_t A_TILE_BYTES = BM * KC * 2;      // 16 KB
 constexpr uint32_t B_TILE_BYTES = B_ROWS * KC * 2;  // 16 KB
 constexpr uint32_t A_BYTES = LIMBS * NKC * A_TILE_BYTES;  // 128 KB
 constexpr uint32_t SMEM_BYTES = A_BYTES + STAGES * B_TILE_BYTES + 1024 /*barriers*/ + 1024 /*align*/;
+// epilogue kinds: residues mod p (Barrett or one Montgomery step), or the
+// fixed-point contraction of the float path (real, or complex realified with
+// GEMM rows 2r / 2r + 1 the real / imaginary parts of output row r)
+constexpr int EPI_BARRETT = 0, EPI_REDC = 1, EPI_F64 = 2, EPI_C128 = 3;
 // exact float -> int for |x| < 2^22: x + 1.5 * 2^23 has unit spacing
 constexpr float MAGIC_F = 12582912.0f;
 constexpr int32_t MAGIC_I = 0x4B400000;
@@ -50,6 +54,11 @@ struct LimbJob {
     uint64_t off;
     int* err;
     int* status;
+    // float epilogue: C is double (Cd, ldc in elements of the output type),
+    // value = sum of digit products * rscale[row] * cscale[column]
+    double* Cd;
+    const double* rscale;
+    const double* cscale;
 };
 
 struct TcParams {
@@ -68,6 +77,9 @@ struct TcParams {
     int redc;
     int* err;
     int* status;
+    double* Cd;             // float epilogue (see LimbJob)
+    const double* rscale;
+    const double* cscale;
 };
 
 __device__ __forceinline__ void split_digits(uint32_t x, uint32_t p, uint32_t half, __nv_bfloat16 (&d)[LIMBS]) {
@@ -185,8 +197,20 @@ __device__ __forceinline__ uint32_t reduce_sum(const FieldU32& f, uint32_t pinv,
 // One CTA of the limb GEMM (see the file comment).  REDC (J.redc): 2^30 <= p
 // < 2^31, the weights carry an extra factor 2^32 and the 64-bit digit sum is
 // reduced by one Montgomery step; otherwise Barrett.
-template <bool REDC>
+// Exact value of the digit-product sum of one output element (float
+// epilogue): the seven group sums are integers below 2^24 in magnitude, so
+// hi (groups 3..6) and lo (groups 0..2) are exact in int64 and the result
+// hi * 2^24 + lo is rounded once.
+__device__ __forceinline__ double fx_digit_value(const int32_t (&y)[GROUPS]) {
+    const int64_t hi = (int64_t)y[3] + ((int64_t)y[4] << 8) + ((int64_t)y[5] << 16) + ((int64_t)y[6] << 24);
+    const int64_t lo = (int64_t)y[0] + ((int64_t)y[1] << 8) + ((int64_t)y[2] << 16);
+    return fma((double)hi, 16777216.0, (double)lo);
+}
+
+template <int EPI>
 __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tmA, const CUtensorMap* tmB) {
+    constexpr bool REDC = EPI == EPI_REDC;
+    constexpr bool FLOAT = EPI == EPI_F64 || EPI == EPI_C128;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte alignment for the 128-byte swizzle atoms
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -321,87 +345,143 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
         int64_t wsum = 0;   // sum of the weights: removes the magic offset in one step
 #pragma unroll
         for (int g = 0; g < GROUPS; ++g) {
-            w[g] = P.w[g];
+            w[g] = FLOAT ? 0 : P.w[g];
             wsum += w[g];
         }
         const uint64_t bias = P.off - (uint64_t)((int64_t)MAGIC_I * wsum);
-        for (int t = 0; t < ntiles; ++t) {
-            const int buf = t & 1;
-            const int64_t col0 = (int64_t)(t0 + t) * BN + 16 * half;
-            uint32_t* crow = P.C + (row_ok ? row : 0) * P.ldc + col0;
-            const int ncols = (int)((P.N - col0) < 16 ? (P.N - col0) : 16);
-            const bool vec = row_ok && ncols == 16 && ((((uintptr_t)crow) & 15) == 0);
-            uint32_t old[16];
-            if (P.overwrite) {
-#pragma unroll
-                for (int c = 0; c < 16; ++c) old[c] = 0u;
-            } else if (vec) {
-#pragma unroll
-                for (int c = 0; c < 16; c += 4) {
-                    const uint4 v = *(const uint4*)(crow + c);
-                    old[c] = v.x; old[c + 1] = v.y; old[c + 2] = v.z; old[c + 3] = v.w;
-                }
-            } else {
-#pragma unroll
-                for (int c = 0; c < 16; ++c) old[c] = (row_ok && c < ncols) ? crow[c] : 0u;
-            }
-            const bool got = ptx::mbar_wait(&acc_full[buf], (t >> 1) & 1, &s_err);
-            if (!__all_sync(0xffffffffu, got)) {  // warp-uniform before the aligned TMEM loads
-                if (lane == 0) flag_error(P, &s_err);
-                break;
-            }
-            ptx::tc_fence_after();
-            uint32_t d[GROUPS][16];
-#pragma unroll
-            for (int g = 0; g < GROUPS; ++g) ptx::tmem_ld16(t_lane + ACC_STRIDE * buf + BN * g, d[g]);
-            ptx::tmem_ld_wait();
-            // accumulator drained: re-zero it and hand it back to the MMA warp
-#pragma unroll
-            for (int g = 0; g < GROUPS; ++g) ptx::tmem_st16_zero(t_lane + ACC_STRIDE * buf + BN * g);
-            ptx::tmem_st_wait();
-            ptx::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&acc_empty[buf]);
-            // exact conversion: for |x| <= 2^22, x + 1.5 * 2^23 is exact and its bit pattern minus
-            // 0x4B400000 is x (full-rate FADD instead of the quarter-rate F2I).  Groups 0, 1, 5, 6 hold
-            // at most two digit products per step and stay within 2^22 for any input; groups 2-4 are
-            // checked.  The weighted sum is formed modulo 2^64; its true value lies in [0, 2^60].
-            float mx = 0.f;
-#pragma unroll
-            for (int g = 2; g <= 4; ++g)
-#pragma unroll
-                for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
-            const bool fast = mx <= 4194304.0f;
-            uint32_t res[16];
-            if (__all_sync(0xffffffffu, fast)) {
+        if constexpr (FLOAT) {
+            // output element (row, col): F64 -> Cd[row * ldc + col];  C128 -> part (row & 1) of
+            // Cd[(row >> 1) * ldc + col] (complex elements, viewed as pairs of doubles)
+            const int64_t orow = (EPI == EPI_C128) ? (row >> 1) : row;
+            const int64_t estride = (EPI == EPI_C128) ? 2 : 1;
+            double* cbase = P.Cd + ((row_ok ? orow : 0) * P.ldc) * estride + ((EPI == EPI_C128) ? (row & 1) : 0);
+            const double rs = row_ok ? P.rscale[row] : 0.0;
+            for (int t = 0; t < ntiles; ++t) {
+                const int buf = t & 1;
+                const int64_t col0 = (int64_t)(t0 + t) * BN + 16 * half;
+                const int ncols = (int)((P.N - col0) < 16 ? (P.N - col0) : 16);
+                double* crow = cbase + col0 * estride;
+                double old[16], cs[16];
 #pragma unroll
                 for (int c = 0; c < 16; ++c) {
-                    uint64_t v = (uint64_t)bias;
-#pragma unroll
-                    for (int g = 0; g < GROUPS; ++g) {
-                        const int32_t y = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F));
-                        v += (uint64_t)((int64_t)y * (int64_t)w[g]);
-                    }
-                    res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
+                    const bool ok = row_ok && c < ncols;
+                    old[c] = (ok && !P.overwrite) ? crow[c * estride] : 0.0;
+                    cs[c] = (c < ncols) ? P.cscale[col0 + c] : 0.0;
                 }
-            } else {
+                const bool got = ptx::mbar_wait(&acc_full[buf], (t >> 1) & 1, &s_err);
+                if (!__all_sync(0xffffffffu, got)) {
+                    if (lane == 0) flag_error(P, &s_err);
+                    break;
+                }
+                ptx::tc_fence_after();
+                uint32_t d[GROUPS][16];
+#pragma unroll
+                for (int g = 0; g < GROUPS; ++g) ptx::tmem_ld16(t_lane + ACC_STRIDE * buf + BN * g, d[g]);
+                ptx::tmem_ld_wait();
+#pragma unroll
+                for (int g = 0; g < GROUPS; ++g) ptx::tmem_st16_zero(t_lane + ACC_STRIDE * buf + BN * g);
+                ptx::tmem_st_wait();
+                ptx::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&acc_empty[buf]);
+                // group sums are exact integers: magic-number conversion where |x| <= 2^22
+                // (groups 0, 1, 5, 6 always; 2-4 checked), F2I otherwise
+                float mx = 0.f;
+#pragma unroll
+                for (int g = 2; g <= 4; ++g)
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
+                const bool fast = __all_sync(0xffffffffu, mx <= 4194304.0f);
 #pragma unroll
                 for (int c = 0; c < 16; ++c) {
-                    uint64_t v = P.off;
+                    int32_t y[GROUPS];
 #pragma unroll
                     for (int g = 0; g < GROUPS; ++g)
-                        v += (uint64_t)((int64_t)__float2int_rn(__uint_as_float(d[g][c])) * (int64_t)w[g]);
-                    res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
+                        y[g] = fast ? (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F)) - MAGIC_I
+                                    : __float2int_rn(__uint_as_float(d[g][c]));
+                    const double v = fx_digit_value(y);
+                    if (row_ok && c < ncols) crow[c * estride] = old[c] + (v * rs) * cs[c];
                 }
             }
-            if (vec) {
-#pragma unroll
-                for (int c = 0; c < 16; c += 4)
-                    *(uint4*)(crow + c) = make_uint4(res[c], res[c + 1], res[c + 2], res[c + 3]);
-            } else if (row_ok) {
-#pragma unroll
-                for (int c = 0; c < 16; ++c)
-                    if (c < ncols) crow[c] = res[c];
+        } else {
+            for (int t = 0; t < ntiles; ++t) {
+                const int buf = t & 1;
+                const int64_t col0 = (int64_t)(t0 + t) * BN + 16 * half;
+                uint32_t* crow = P.C + (row_ok ? row : 0) * P.ldc + col0;
+                const int ncols = (int)((P.N - col0) < 16 ? (P.N - col0) : 16);
+                const bool vec = row_ok && ncols == 16 && ((((uintptr_t)crow) & 15) == 0);
+                uint32_t old[16];
+                if (P.overwrite) {
+    #pragma unroll
+                    for (int c = 0; c < 16; ++c) old[c] = 0u;
+                } else if (vec) {
+    #pragma unroll
+                    for (int c = 0; c < 16; c += 4) {
+                        const uint4 v = *(const uint4*)(crow + c);
+                        old[c] = v.x; old[c + 1] = v.y; old[c + 2] = v.z; old[c + 3] = v.w;
+                    }
+                } else {
+    #pragma unroll
+                    for (int c = 0; c < 16; ++c) old[c] = (row_ok && c < ncols) ? crow[c] : 0u;
+                }
+                const bool got = ptx::mbar_wait(&acc_full[buf], (t >> 1) & 1, &s_err);
+                if (!__all_sync(0xffffffffu, got)) {  // warp-uniform before the aligned TMEM loads
+                    if (lane == 0) flag_error(P, &s_err);
+                    break;
+                }
+                ptx::tc_fence_after();
+                uint32_t d[GROUPS][16];
+    #pragma unroll
+                for (int g = 0; g < GROUPS; ++g) ptx::tmem_ld16(t_lane + ACC_STRIDE * buf + BN * g, d[g]);
+                ptx::tmem_ld_wait();
+                // accumulator drained: re-zero it and hand it back to the MMA warp
+    #pragma unroll
+                for (int g = 0; g < GROUPS; ++g) ptx::tmem_st16_zero(t_lane + ACC_STRIDE * buf + BN * g);
+                ptx::tmem_st_wait();
+                ptx::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&acc_empty[buf]);
+                // exact conversion: for |x| <= 2^22, x + 1.5 * 2^23 is exact and its bit pattern minus
+                // 0x4B400000 is x (full-rate FADD instead of the quarter-rate F2I).  Groups 0, 1, 5, 6 hold
+                // at most two digit products per step and stay within 2^22 for any input; groups 2-4 are
+                // checked.  The weighted sum is formed modulo 2^64; its true value lies in [0, 2^60].
+                float mx = 0.f;
+    #pragma unroll
+                for (int g = 2; g <= 4; ++g)
+    #pragma unroll
+                    for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
+                const bool fast = mx <= 4194304.0f;
+                uint32_t res[16];
+                if (__all_sync(0xffffffffu, fast)) {
+    #pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        uint64_t v = (uint64_t)bias;
+    #pragma unroll
+                        for (int g = 0; g < GROUPS; ++g) {
+                            const int32_t y = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F));
+                            v += (uint64_t)((int64_t)y * (int64_t)w[g]);
+                        }
+                        res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
+                    }
+                } else {
+    #pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        uint64_t v = P.off;
+    #pragma unroll
+                        for (int g = 0; g < GROUPS; ++g)
+                            v += (uint64_t)((int64_t)__float2int_rn(__uint_as_float(d[g][c])) * (int64_t)w[g]);
+                        res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
+                    }
+                }
+                if (vec) {
+    #pragma unroll
+                    for (int c = 0; c < 16; c += 4)
+                        *(uint4*)(crow + c) = make_uint4(res[c], res[c + 1], res[c + 2], res[c + 3]);
+                } else if (row_ok) {
+    #pragma unroll
+                    for (int c = 0; c < 16; ++c)
+                        if (c < ncols) crow[c] = res[c];
+                }
             }
         }
     }
@@ -411,7 +491,7 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
     if (warp == 1) ptx::tmem_dealloc(tmem, TMEM_COLS);
 }
 
-template <bool REDC>
+template <int EPI>
 static __global__ void __launch_bounds__(THREADS, 1)
     limb_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const __grid_constant__ TcParams P) {
@@ -435,7 +515,10 @@ static __global__ void __launch_bounds__(THREADS, 1)
     J.off = P.off;
     J.err = P.err;
     J.status = P.status;
-    limb_cta<REDC>(J, &tmA, &tmB);
+    J.Cd = P.Cd;
+    J.rscale = P.rscale;
+    J.cscale = P.cscale;
+    limb_cta<EPI>(J, &tmA, &tmB);
 }
 
 }  // namespace tc

@@ -186,7 +186,7 @@ int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t
     P.err = err;
     P.status = status;
     P.redc = redc ? 1 : 0;
-    auto kern = redc ? limb_gemm_kernel<true> : limb_gemm_kernel<false>;
+    auto kern = redc ? limb_gemm_kernel<EPI_REDC> : limb_gemm_kernel<EPI_BARRETT>;
     LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
     if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }

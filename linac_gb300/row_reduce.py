@@ -89,7 +89,7 @@ def rref_host_call(host: np.ndarray, p: int, out: np.ndarray, flags: int = 0,
 
 @timeit
 def cuda_row_reduce(matrix, field_characteristic=0, verbose=False, _real=None, _mod64=None,
-                    return_pivots=False, out=None):
+                    return_pivots=False, out=None, mixed=False):
     r"""Reduced row-echelon form on the GPU.
 
     Args:
@@ -100,6 +100,9 @@ def cuda_row_reduce(matrix, field_characteristic=0, verbose=False, _real=None, _
         return_pivots (bool): also return the list of pivot columns.
         out (ndarray, optional): destination of the result (shape of matrix,
             dtype of the field).
+        mixed (bool): real / complex matrices only -- trailing updates on the
+            tensor cores in 31-bit fixed point, FP64 panels, FP64 refinement
+            of the result (``linac_gb300._lib.mixed_report()`` describes it).
     """
     matrix = np.asarray(matrix)
     if matrix.ndim != 2:
@@ -113,7 +116,12 @@ def cuda_row_reduce(matrix, field_characteristic=0, verbose=False, _real=None, _
         raise ValueError(f"out must have shape {host.shape} and dtype {dtype}")
     if verbose:
         _lib.kernel_timing(True)
-    pivots, rank = rref_host_call(host, p, out)
+    flags = 0
+    if mixed:
+        if p != 0:
+            raise ValueError("mixed precision applies to real / complex matrices (field_characteristic=0)")
+        flags |= _lib.LNC_FLAG_MIXED
+    pivots, rank = rref_host_call(host, p, out, flags=flags)
     if verbose:
         for name, kc in (("panel", _lib.KC_PANEL), ("trailing update", _lib.KC_TRAILING),
                          ("gather", _lib.KC_GATHER)):

@@ -51,6 +51,9 @@ WORKLOADS = {
     "rref_u32_20000": dict(m=20000, n=20000, p=P31, dtype="u32"),
     "rref_u32_8192": dict(m=8192, n=8192, p=P31, dtype="u32"),
     "rref_u32_4096": dict(m=4096, n=4096, p=P31, dtype="u32"),
+    "rref_u64_8000": dict(m=8000, n=8000, p=2**61 - 1, dtype="u64"),
+    # 512 x 640 of rank 384 built as B.C mod 2^31-1 (seed 0), checked against the oracle
+    "config1": dict(m=512, n=640, p=P31, dtype="u32", config1=True),
     # uneven batch: m ~ U[64, 2048], n = round(m U[0.8, 1.25]), rank deficit ~ U[0, 10%],
     # a prime per matrix from the 64 largest primes below 2^31, built as B.C on the device
     "batch4096": dict(count=4096, m_lo=64, m_hi=2048, dtype="u32", batch=True),
@@ -176,11 +179,12 @@ def measured_peaks():
 
 def gen_matrix(m: int, n: int, p: int, seed: int, out: np.ndarray | None = None) -> np.ndarray:
     rng = np.random.default_rng(seed)
-    A = out if out is not None else np.empty((m, n), dtype=np.uint32)
+    dt = np.uint32 if p < 2**32 else np.uint64
+    A = out if out is not None else np.empty((m, n), dtype=dt)
     chunk = max(1, (1 << 26) // max(n, 1))
     for r0 in range(0, m, chunk):
         r1 = min(m, r0 + chunk)
-        A[r0:r1] = rng.integers(0, p, size=(r1 - r0, n), dtype=np.uint32)
+        A[r0:r1] = rng.integers(0, p, size=(r1 - r0, n), dtype=dt)
     return A
 
 
@@ -226,11 +230,18 @@ def run_ours(args, dist: Dist):
     wl = WORKLOADS[args.workload]
     m, n, p = wl["m"], wl["n"], wl["p"]
     L = _lib.lib()
-    nbytes = m * n * 4
+    u64 = wl["dtype"] == "u64"
+    dt = np.uint64 if u64 else np.uint32
+    code = _lib.LNC_U64 if u64 else _lib.LNC_U32
+    nbytes = m * n * np.dtype(dt).itemsize
     seed = 1234 + dist.rank
-    host_in = pinned_empty((m, n), np.uint32)
-    gen_matrix(m, n, p, seed, out=host_in)
-    host_out = pinned_empty((m, n), np.uint32)
+    host_in = pinned_empty((m, n), dt)
+    if wl.get("config1"):
+        from linac_gb300 import workloads
+        host_in[:] = workloads.config1()[0]
+    else:
+        gen_matrix(m, n, p, seed, out=host_in)
+    host_out = pinned_empty((m, n), dt)
 
     d_src = _lib.DeviceBuffer(nbytes)
     d_work = _lib.DeviceBuffer(nbytes)
@@ -244,7 +255,7 @@ def run_ours(args, dist: Dist):
 
     def step():
         _lib.check(L.lnc_memcpy_d2d(d_work.ptr, d_src.ptr, nbytes, stream.handle))
-        _lib.check(L.lnc_rref_device(_lib.LNC_U32, m, n, p, 0.0, d_work.ptr, n, d_out.ptr, n, d_piv.ptr,
+        _lib.check(L.lnc_rref_device(code, m, n, p, 0.0, d_work.ptr, n, d_out.ptr, n, d_piv.ptr,
                                      d_rank.ptr, stream.handle, args.flags))
 
     for _ in range(args.warmup):
@@ -286,10 +297,19 @@ def run_ours(args, dist: Dist):
     piv = np.empty(kmax, dtype=np.int64)
     d_piv.download(piv, stream.handle)
     rank = int(np.count_nonzero(piv >= 0))
-    ident_ok = bool(rank == n and np.all(piv == np.arange(n)))
-    if ident_ok:
-        diag = host_out.reshape(-1)[:: n + 1]
-        ident_ok = bool(np.all(diag == 1) and int(np.count_nonzero(host_out)) == n)
+    if wl.get("config1"):
+        import hashlib
+        import oracle
+        R_ref, piv_ref, rank_ref = oracle.rref_modp(host_in, p)
+        ident_ok = bool(rank == rank_ref == 384 and list(piv[:rank]) == list(piv_ref)
+                        and np.array_equal(host_out.astype(np.uint64), R_ref))
+        result_hash = hashlib.sha256(np.ascontiguousarray(host_out).tobytes()).hexdigest()[:16]
+    else:
+        ident_ok = bool(rank == n and np.all(piv == np.arange(n)))
+        if ident_ok:
+            diag = host_out.reshape(-1)[:: n + 1]
+            ident_ok = bool(np.all(diag == 1) and int(np.count_nonzero(host_out)) == n)
+        result_hash = None
 
     t_max = dist.max(total_ms / 1000.0)
     solves = dist.sum(float(args.steps))
@@ -307,18 +327,19 @@ def run_ours(args, dist: Dist):
 
     # ---- roofline of the dominant kernel class ----
     peaks = measured_peaks()
-    W = rref_work(m, n, range(n)) if ident_ok else rref_work(m, n, piv[piv >= 0])
+    W = rref_work(m, n, piv[piv >= 0])
     dom = max(("panel", "trailing"), key=lambda k: kt[k][1])
     work = kt_work[dom]
     if dom == "trailing":
-        if args.flags & _lib.LNC_FLAG_SIMT_TRAILING:
+        if (args.flags & _lib.LNC_FLAG_SIMT_TRAILING) or u64:
             # SIMT integer contraction: report its HBM traffic against the copy roofline
             launches = max(1, kt["trailing"][0])
-            bytes_per_launch = trailing_bytes(m, n, 128) / launches
-            achieved = trailing_bytes(m, n, 128) / (kt["trailing"][1] / 1e3) / 1e9
+            elt = np.dtype(dt).itemsize
+            bytes_per_launch = trailing_bytes(m, n, 128) * elt / 4 / launches
+            achieved = trailing_bytes(m, n, 128) * elt / 4 / (kt["trailing"][1] / 1e3) / 1e9
             roof = {"bound": "hbm", "kernel": "trailing_simt_kernel", "achieved": achieved,
                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                    "traffic": traffic_per_launch("trailing_simt"),
+                    "traffic": traffic_per_launch(args.workload, "trailing_simt"),
                     "peak_source": f"{peaks['source']} copy bandwidth",
                     "bytes_per_launch": bytes_per_launch}
         else:
@@ -327,7 +348,7 @@ def run_ours(args, dist: Dist):
             achieved = flops / (kt["trailing"][1] / 1e3) / 1e12
             peak = peaks["bf16_tflops_sustained"]
             roof = {"bound": "tensor", "kernel": "tc::limb_gemm_kernel", "achieved": achieved, "peak": peak,
-                    "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic_per_launch("limb_gemm"),
+                    "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic_per_launch(args.workload, "limb_gemm"),
                     "peak_source": f"{peaks['source']} bf16 sustained (kernel timed inside a long solve)",
                     "work_unit": "field multiply-adds m*N*128 per launch, x 2*4*4 bf16 flops",
                     "flops_per_launch": flops / max(1, kt["trailing"][0])}
@@ -335,7 +356,7 @@ def run_ours(args, dist: Dist):
         achieved = work / (kt["panel"][1] / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": "panel (cand_panel_kernel / panel_kernel)", "achieved": achieved,
                 "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                "traffic": traffic_per_launch("panel"), "peak_source": f"{peaks['source']} copy bandwidth",
+                "traffic": traffic_per_launch(args.workload, "panel"), "peak_source": f"{peaks['source']} copy bandwidth",
                 "note": "latency-bound: one pivot step per column"}
 
     line = {
@@ -349,14 +370,18 @@ def run_ours(args, dist: Dist):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": value / (1.0 / PUBLISHED_20K_SECONDS) if args.workload == "rref_u32_20000" else None,
-        "dtype": "u32",
-        "data": "synthetic (uniform residues mod 2^31-1, seed 1234+rank)",
-        "config": {"workload": f"rref_u32_{m}x{n}_p2^31-1", "m": m, "n": n, "p": p,
+        "dtype": wl["dtype"],
+        "data": ("synthetic (B.C mod 2^31-1, B 512x384 and C 384x640 uniform, seed 0)" if wl.get("config1")
+                 else f"synthetic (uniform residues mod p, seed 1234+rank)"),
+        "config": {"workload": (f"rref_{wl['dtype']}_{m}x{n}_p{'2^61-1' if u64 else '2^31-1'}"
+                                + ("_rank384" if wl.get("config1") else "")), "m": m, "n": n, "p": p,
                    "parallelism": f"replicas x{dist.world}", "panel_width": 128,
-                   "trailing": "simt" if args.flags & _lib.LNC_FLAG_SIMT_TRAILING else "tensor_core",
-                   "panel": "exhaustive" if args.flags & (_lib.LNC_FLAG_ROBUST_PANEL | _lib.LNC_FLAG_SIMT_TRAILING)
+                   "trailing": "simt" if (args.flags & _lib.LNC_FLAG_SIMT_TRAILING) or u64 else "tensor_core",
+                   "panel": "exhaustive" if (args.flags & (_lib.LNC_FLAG_ROBUST_PANEL | _lib.LNC_FLAG_SIMT_TRAILING)) or u64
                    else "candidate block + exhaustive fallback",
-                   "l2": "input 1.6 GB > L2 (129 MB); no flush needed"},
+                   "l2": (f"input {nbytes / 1e6:.0f} MB > L2 (129 MB); no flush needed" if nbytes > 129e6
+                          else f"input {nbytes / 1e6:.1f} MB fits L2: inputs restored by a D2D copy each step")},
+        "result_sha256_16": result_hash,
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "min": float(min(lat)), "max": float(max(lat))},
         "bit_exact": ident_ok,
@@ -369,7 +394,17 @@ def run_ours(args, dist: Dist):
         "host_wall_s": t_host,
         "work_field_macs_per_solve": W,
     }
-    if dist.rank == 0 and not args.no_cpu_baseline:
+    if dist.rank == 0 and not args.no_cpu_baseline and wl.get("config1"):
+        import oracle
+        reps, t0 = 0, time.perf_counter()
+        while reps < 3 or time.perf_counter() - t0 < 2.0:
+            oracle.rref_modp(host_in, p)
+            reps += 1
+        t_full = (time.perf_counter() - t0) / reps
+        line["cpu_baseline"] = {"value": 1.0 / t_full, "unit": "solves/s", "cores": oracle.default_threads(),
+                                "kind": "port", "sample": f"{reps} whole solves of the same 512x640 matrix",
+                                "extrapolated_s_per_solve": t_full}
+    elif dist.rank == 0 and not args.no_cpu_baseline:
         v, threads, desc, t_full = cpu_sample(m, n, p, seed, target_s=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": threads, "kind": "port", "sample": desc,
                                 "extrapolated_s_per_solve": t_full}
@@ -397,16 +432,18 @@ def trailing_bytes(m: int, n: int, b: int) -> float:
     return tot
 
 
-def traffic_per_launch(kernel: str):
-    path = os.path.join(ROOT, "profiles", "traffic.json")
-    if not os.path.exists(path):
-        return None
-    try:
-        with open(path) as f:
-            d = json.load(f)
-        return d.get(kernel)
-    except (OSError, ValueError):
-        return None
+# DRAM bytes (read + write) per launch of the dominant kernel, averaged over
+# the launches of one ncu capture of the same workload (dram__bytes_read.sum +
+# dram__bytes_write.sum, one pass): profiles/launches_rref_u32_20000.md and
+# profiles/launches_rref_u64_8000.md
+PROFILED_TRAFFIC = {
+    ("rref_u32_20000", "limb_gemm"): 534.0e6,
+    ("rref_u64_8000", "trailing_simt"): 465.4e6,
+}
+
+
+def traffic_per_launch(workload: str, kernel: str):
+    return PROFILED_TRAFFIC.get((workload, kernel))
 
 
 # ---------------------------------------------------------------------------

@@ -331,7 +331,7 @@ def run_ours(args, dist: Dist):
     dom = max(("panel", "trailing"), key=lambda k: kt[k][1])
     work = kt_work[dom]
     if dom == "trailing":
-        if (args.flags & _lib.LNC_FLAG_SIMT_TRAILING) or u64:
+        if args.flags & _lib.LNC_FLAG_SIMT_TRAILING:
             # SIMT integer contraction: report its HBM traffic against the copy roofline
             launches = max(1, kt["trailing"][0])
             elt = np.dtype(dt).itemsize
@@ -343,14 +343,16 @@ def run_ours(args, dist: Dist):
                     "peak_source": f"{peaks['source']} copy bandwidth",
                     "bytes_per_launch": bytes_per_launch}
         else:
-            # tensor-core limb GEMM: 2 * L^2 bf16 flops per field multiply-add (L = 4 digits)
-            flops = 2.0 * 16.0 * work
+            # tensor-core limb GEMM: 2 * L^2 bf16 flops per field multiply-add (L = 4 digits, 8 for uint64)
+            flops = 2.0 * (64.0 if u64 else 16.0) * work
             achieved = flops / (kt["trailing"][1] / 1e3) / 1e12
             peak = peaks["bf16_tflops_sustained"]
-            roof = {"bound": "tensor", "kernel": "tc::limb_gemm_kernel", "achieved": achieved, "peak": peak,
+            roof = {"bound": "tensor", "kernel": "tc64::limb64_gemm_kernel" if u64 else "tc::limb_gemm_kernel",
+                    "achieved": achieved, "peak": peak,
                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic_per_launch(args.workload, "limb_gemm"),
                     "peak_source": f"{peaks['source']} bf16 sustained (kernel timed inside a long solve)",
-                    "work_unit": "field multiply-adds m*N*128 per launch, x 2*4*4 bf16 flops",
+                    "work_unit": ("field multiply-adds m*N*64 per launch, x 2*8*8 bf16 flops" if u64
+                                  else "field multiply-adds m*N*128 per launch, x 2*4*4 bf16 flops"),
                     "flops_per_launch": flops / max(1, kt["trailing"][0])}
     else:
         achieved = work / (kt["panel"][1] / 1e3) / 1e9
@@ -375,8 +377,9 @@ def run_ours(args, dist: Dist):
                  else f"synthetic (uniform residues mod p, seed 1234+rank)"),
         "config": {"workload": (f"rref_{wl['dtype']}_{m}x{n}_p{'2^61-1' if u64 else '2^31-1'}"
                                 + ("_rank384" if wl.get("config1") else "")), "m": m, "n": n, "p": p,
-                   "parallelism": f"replicas x{dist.world}", "panel_width": 128,
-                   "trailing": "simt" if (args.flags & _lib.LNC_FLAG_SIMT_TRAILING) or u64 else "tensor_core",
+                   "parallelism": f"replicas x{dist.world}", "panel_width": 64 if u64 else 128,
+                   "trailing": "simt" if args.flags & _lib.LNC_FLAG_SIMT_TRAILING else
+                   ("tensor_core (8 digits)" if u64 else "tensor_core (4 digits)"),
                    "panel": "exhaustive" if (args.flags & (_lib.LNC_FLAG_ROBUST_PANEL | _lib.LNC_FLAG_SIMT_TRAILING)) or u64
                    else "candidate block + exhaustive fallback",
                    "l2": (f"input {nbytes / 1e6:.0f} MB > L2 (129 MB); no flush needed" if nbytes > 129e6

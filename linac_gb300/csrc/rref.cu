@@ -473,6 +473,9 @@ int plan_rref(int64_t m, int64_t n, RrefPlan* plan) {
         set_error("matrix too tall for the panel kernel: %lld rows", (long long)m);
         return LNC_ERR_UNSUPPORTED;
     }
+    if constexpr (F::kDtype == 2) {  // 64-bit residues: the tensor-core update takes 64-column panels
+        if (trailing_tc_u64_available()) b = std::min(b, kMaxPanelU64Tc);
+    }
     plan->G = G;
     plan->rows_per_cta = R;
     plan->b = b;

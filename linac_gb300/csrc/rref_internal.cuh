@@ -205,9 +205,16 @@ int launch_split_g(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, uint32
 int launch_check_missed(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, int bw, const uint8_t* row_used,
                         const uint32_t* pivmask, int* missed, cudaStream_t s);
 
+// Tensor-core trailing update for 64-bit residues (trailing_tc64.cu); panels of <= 64 columns
+int trailing_update_tc_u64(const TrailingCtx<FieldU64>& t, cudaStream_t s);
+size_t trailing_tc_u64_scratch(int64_t m, int64_t n);
+bool trailing_tc_u64_available();
+constexpr int kMaxPanelU64Tc = 64;
+
 template <class F>
 inline size_t trailing_extra_scratch(int64_t m, int64_t n, const RrefPlan& pl) {
     if constexpr (F::kDtype == 1) return trailing_tc_u32_scratch(m, n, pl.b);
+    if constexpr (F::kDtype == 2) return trailing_tc_u64_available() ? trailing_tc_u64_scratch(m, n) : 0;
     return 0;
 }
 
@@ -230,6 +237,9 @@ template <class F>
 inline int trailing_update(const TrailingCtx<F>& t, cudaStream_t s) {
     if constexpr (F::kDtype == 1) {
         if (!t.force_simt && trailing_tc_u32_available()) return trailing_update_tc_u32(t, s);
+    }
+    if constexpr (F::kDtype == 2) {
+        if (!t.force_simt && t.b <= kMaxPanelU64Tc && trailing_tc_u64_available()) return trailing_update_tc_u64(t, s);
     }
     if constexpr (F::kDtype == 3 || F::kDtype == 4) {
         if (t.fx) return trailing_update_fx<F>(t, s);

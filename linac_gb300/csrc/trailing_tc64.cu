@@ -1,0 +1,82 @@
+// Tensor-core trailing update for 64-bit residues (host side of
+// tc64_kernels.cuh): digit split of E, gather + digit split of the pivot rows
+// (zeroed in A), and the limb GEMM  A[:, T] += E A[P, T] (mod p).
+#include <cuda.h>
+
+#include "tc64_kernels.cuh"
+
+namespace lnc {
+
+int tc_make_map_bf16(CUtensorMap* map, void* base, uint64_t inner, uint64_t outer, uint32_t box_inner,
+                     uint32_t box_outer);
+
+namespace {
+int m_pad64(int64_t m) { return (int)((m + tc64::BM - 1) / tc64::BM * tc64::BM); }
+int n_tiles64(int64_t n) { return (int)((n + tc64::BN - 1) / tc64::BN); }
+size_t el64_bytes(int64_t m) { return ((size_t)tc64::LIMBS * m_pad64(m) * tc64::KMAX * 2 + 1023) / 1024 * 1024; }
+size_t bs64_bytes(int64_t n) {
+    return ((size_t)n_tiles64(n) * tc64::B_ROWS * tc64::KMAX * 2 + 1023) / 1024 * 1024;
+}
+}  // namespace
+
+bool trailing_tc_u64_available() {
+    DeviceInfo di;
+    return trailing_tc_u32_available() && device_info(&di) == LNC_OK && di.smem_optin >= (int)tc64::SMEM_BYTES;
+}
+
+size_t trailing_tc_u64_scratch(int64_t m, int64_t n) { return el64_bytes(m) + bs64_bytes(n) + 1024; }
+
+int trailing_update_tc_u64(const TrailingCtx<FieldU64>& t, cudaStream_t s) {
+    using namespace tc64;
+    if (t.b > KMAX) { set_error("64-bit tensor-core update needs panels of at most %d columns", KMAX); return LNC_ERR_INVALID; }
+    const uint64_t p = t.f.p;
+    const int m_pad = m_pad64(t.m);
+    const int n_tiles = n_tiles64(t.N);
+    unsigned char* base = (unsigned char*)(((uintptr_t)t.extra + 1023) & ~(uintptr_t)1023);
+    __nv_bfloat16* EL = (__nv_bfloat16*)base;
+    __nv_bfloat16* BS = (__nv_bfloat16*)(base + el64_bytes(t.m));
+    {
+        const int grid = (int)std::min<int64_t>(((int64_t)m_pad * KMAX + 255) / 256, 8192);
+        split_e64_kernel<<<grid, 256, 0, s>>>(t.E, t.ldE, t.m, m_pad, p, t.panel_k, EL);
+        LNC_CHECK_LAUNCH("split_e64_kernel");
+    }
+    gather_split_b64_kernel<<<n_tiles, 256, 0, s>>>(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, p, BS);
+    LNC_CHECK_LAUNCH("gather_split_b64_kernel");
+    CUtensorMap mapA, mapB;
+    int rc = tc_make_map_bf16(&mapA, EL, KMAX, (uint64_t)LIMBS * m_pad, KC, BM);
+    if (!rc) rc = tc_make_map_bf16(&mapB, BS, KMAX, (uint64_t)n_tiles * B_ROWS, KC, B_ROWS);
+    if (rc) return rc;
+    Params64 P{};
+    P.C = t.A + t.j1;
+    P.ldc = t.lda;
+    P.m = t.m;
+    P.N = t.N;
+    P.m_pad = m_pad;
+    P.n_tiles = n_tiles;
+    P.panel_k = t.panel_k;
+    P.f = t.f;
+    {
+        // w_s = 2^(8 s) 2^64 mod p (centred): one Montgomery step of the weighted sum gives sum y_s 2^(8 s)
+        unsigned __int128 x = (((unsigned __int128)1) << 64) % p;
+        for (int g = 0; g < GROUPS; ++g) {
+            const uint64_t xv = (uint64_t)x;
+            P.w[g] = (xv > p / 2) ? -(int64_t)(p - xv) : (int64_t)xv;
+            x = (x * 256) % p;
+        }
+        const unsigned __int128 two91 = ((unsigned __int128)1) << 91;
+        const unsigned __int128 off = ((two91 + p - 1) / p) * p;
+        P.off_lo = (uint64_t)off;
+        P.off_hi = (uint64_t)(off >> 64);
+    }
+    P.err = t.err;
+    P.status = t.status;
+    LNC_CUDA(cudaFuncSetAttribute(limb64_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+    dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
+    if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }
+    ScopedKernelTimer kt(KC_TRAILING, s, t.predicated ? 0.0 : (double)t.m * (double)t.N * (double)t.b);
+    limb64_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(mapA, mapB, P);
+    LNC_CHECK_LAUNCH("limb64_gemm_kernel");
+    return LNC_OK;
+}
+
+}  // namespace lnc

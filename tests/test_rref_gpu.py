@@ -234,3 +234,24 @@ def test_panel_paths_agree_on_adversarial_inputs(flags, m, n, r, p):
     R_ref, piv_ref, _ = oracle.rref_modp(A, p)
     assert np.array_equal(out.astype(np.uint64), R_ref)
     assert piv == piv_ref
+
+
+@pytest.mark.parametrize("flags", [0, _lib.LNC_FLAG_SIMT_TRAILING])
+@pytest.mark.parametrize("m,n,p", [(700, 900, 2**61 - 1), (900, 600, 2**32 + 15), (520, 520, 2**64 - 59)])
+def test_u64_tensor_core_update_vs_oracle(flags, m, n, p):
+    """64-bit residues: eight-digit limb contraction (default) and the SIMT
+    update agree with the oracle, including entries at the digit extremes
+    (p - 1, (p - 1) / 2, (p + 1) / 2) and rank deficiency."""
+    rng = np.random.default_rng(m * 7 + n)
+    r = min(m, n) - 37
+    Bf = rng.integers(0, 2**63, size=(m, r), dtype=np.uint64) % np.uint64(p)
+    Cf = rng.integers(0, 2**63, size=(r, n), dtype=np.uint64) % np.uint64(p)
+    A = oracle.matmul_modp(Bf, Cf, p)
+    A[:40, 100:300] = np.uint64(p - 1)
+    A[40:80, 300:500] = np.uint64((p - 1) // 2)
+    A[80:90] = np.uint64((p + 1) // 2)
+    out = np.empty_like(A)
+    piv, rank = rref_host_call(A, p, out, flags=flags)
+    R_ref, piv_ref, _ = oracle.rref_modp(A, p)
+    assert np.array_equal(out, R_ref)
+    assert piv == piv_ref

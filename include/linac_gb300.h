@@ -205,6 +205,39 @@ int lnc_matmul_modp_device(int dtype, int64_t m, int64_t k, int64_t n, uint64_t 
  * counterpart (linac's float path is FP64 only, linac/row_reduce.cu:55-270). */
 int lnc_mixed_report(int* iterations, double* last_correction, int* redone_fp64);
 
+/* ---- incremental RREF --------------------------------------------------------- */
+/*
+ * RREF of [rows so far; k new rows] from the RREF of the rows so far, over F_p
+ * with 32-bit residues.  dev_rref (r x n, ld_rref) holds the r non-zero RREF
+ * rows with pivot columns dev_pivot_cols[0..r) (increasing) and is
+ * overwritten with those rows cleared in the new pivot columns; dev_new is
+ * k x n (ld_new, residues); dev_out ((r + k) x n, ld_out) receives the RREF of
+ * the stacked rows, zero rows after the rank; its pivot columns and rank go to
+ * dev_out_pivot_cols (r + k entries) and dev_out_rank.  Costs k r n + r s n
+ * multiply-adds (s new pivots) plus a k-row RREF; synchronises the stream
+ * once.  No reference counterpart: linac re-reduces the grown matrix from
+ * scratch (linac/vector_spaces/over_function_fields.py:74-101).
+ */
+int lnc_rref_append_device(int dtype, int64_t r, int64_t k, int64_t n, uint64_t p, void* dev_rref,
+                           int64_t ld_rref, const int64_t* dev_pivot_cols, const void* dev_new,
+                           int64_t ld_new, void* dev_out, int64_t ld_out, int64_t* dev_out_pivot_cols,
+                           int64_t* dev_out_rank, void* stream);
+
+/* ---- null space ------------------------------------------------------------- */
+/*
+ * Canonical null-space basis of an RREF R (r x n, ld_rref, device) with pivot
+ * columns dev_pivot_cols[0..r) (increasing): out (n x (n - r), ld_out, device,
+ * R's element type) with out[Pc[t], j] = R[t, Nc[j]] and out[Nc[i], j] =
+ * -[i == j] (-1 is p - 1 over F_p; p = 2^32 for uint32 or 0 for uint64 writes
+ * the all-ones word, a marker no residue equals), Nc the non-pivot columns in
+ * order.
+ * Replaces canonical_kernel_from_row_reduced_echelon_form
+ * (linac/linear_algebra_tools.py:54-63), which runs on the host.
+ */
+int lnc_canonical_kernel_device(int dtype, int64_t r, int64_t n, uint64_t p, const void* dev_rref,
+                                int64_t ld_rref, const int64_t* dev_pivot_cols, void* dev_out,
+                                int64_t ld_out, void* stream);
+
 /* ---- monomial loader --------------------------------------------------------- */
 /*
  * out[r, c] = prod_{t<degree} bases[r, lindices[c, t]] (mod p for LNC_U32 /

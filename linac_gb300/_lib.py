@@ -99,6 +99,9 @@ _SIGNATURES = {
     "lnc_load_matrix_device": ([_int, _i64, _i64, _i64, _i64, _u64, _vp, _vp, _vp, _i64, _vp], _int),
     "lnc_fill_uniform_modp": ([_vp, _i64, _u64, _u64, _int, _vp], _int),
     "lnc_mixed_report": ([_vp, _vp, _vp], _int),
+    "lnc_canonical_kernel_device": ([_int, _i64, _i64, _u64, _vp, _i64, _vp, _vp, _i64, _vp], _int),
+    "lnc_rref_append_device": ([_int, _i64, _i64, _i64, _u64, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp],
+                               _int),
     "lnc_matmul_modp_device": ([_int, _i64, _i64, _i64, _u64, _vp, _i64, _vp, _i64, _vp, _i64, _vp], _int),
 }
 

@@ -328,7 +328,7 @@ static int record_batch(BatchPlan& P, cudaStream_t s) {
     const unsigned gx_rows = (unsigned)std::min<int64_t>(std::max<int64_t>(1, (P.max_rows * 128 + 255) / 256), 64);
     batch_prepare_kernel<<<dim3(64, gy), 256, 0, s>>>(P.d_desc);
     ++launches;
-    const size_t cand_smem = (size_t)(P.smax | 1) * kMaxPanel * 4 + kMaxPanel * 4 + 256 * 4;
+    const size_t cand_smem = (size_t)(P.smax | 1) * kMaxPanel * 4 + 2 * kMaxPanel * 4 + 256 * 4;
     for (int q = 0; q < P.steps; ++q) {
         const int na = P.active_cnt[q];
         const int* act = P.d_prefix + P.active_off[q];
@@ -541,7 +541,7 @@ static int plan_create(const lnc_batch_matrix* mats, int64_t count, int tpc, int
         return rc;
     }
     // ---- capture the whole batch into one graph
-    const size_t cand_smem = (size_t)(P->smax | 1) * kMaxPanel * 4 + kMaxPanel * 4 + 256 * 4;
+    const size_t cand_smem = (size_t)(P->smax | 1) * kMaxPanel * 4 + 2 * kMaxPanel * 4 + 256 * 4;
     LNC_CUDA(cudaFuncSetAttribute(batch_cand_kernel<ArithSmall, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)cand_smem));
     LNC_CUDA(cudaFuncSetAttribute(batch_cand_kernel<ArithMont, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,

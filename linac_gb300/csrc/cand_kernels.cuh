@@ -50,9 +50,10 @@ __device__ __forceinline__ uint32_t cp_inverse(const Mont32& M, uint32_t a) {
     }
 }
 
-// Arithmetic policies of the candidate panel.  `prep` turns a normalised
-// pivot-row value into the form its multiplier uses, `mulp(f, prep(v))` is
-// f * v mod p, `mul` multiplies two ordinary residues.
+// Arithmetic policies of the candidate panel.  `prep` / `aux` turn a
+// normalised pivot-row value v into the form(s) the update uses, and
+// `mulsub(x, f, prep(v), aux(v))` is x - f v mod p; `mul` multiplies two
+// ordinary residues.
 struct ArithSmall {  // odd p < 2^31: 32-bit Montgomery, reductions by unsigned min
     Mont32 M;
     __device__ ArithSmall(const decltype(CandArgs::M)& c) : M(c) {}
@@ -63,8 +64,18 @@ struct ArithSmall {  // odd p < 2^31: 32-bit Montgomery, reductions by unsigned 
         return min(u, u - M.p);
     }
     __device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b) const { return red((uint64_t)a * b); }
-    __device__ __forceinline__ uint32_t prep(uint32_t v) const { return montmul(v, M.r2); }
-    __device__ __forceinline__ uint32_t mulp(uint32_t f, uint32_t vp) const { return montmul(f, vp); }
+    __device__ __forceinline__ uint32_t prep(uint32_t v) const { return v; }
+    // Shoup's constant of a fixed multiplier v: floor(v 2^32 / p)
+    __device__ __forceinline__ uint32_t aux(uint32_t v) const { return (uint32_t)(((uint64_t)v << 32) / M.p); }
+    // x - f v mod p with v's Shoup constant vs: q = floor(f vs / 2^32) undershoots f v / p by at
+    // most 1, so f v - q p lies in [0, 2p) (computed mod 2^32; 2p < 2^32)
+    __device__ __forceinline__ uint32_t mulsub(uint32_t x, uint32_t f, uint32_t v, uint32_t vs) const {
+        const uint32_t q = __umulhi(f, vs);
+        uint32_t r = f * v - q * M.p;
+        r = min(r, r - M.p);
+        const uint32_t d = x - r;
+        return min(d, d + M.p);
+    }
     __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return montmul(montmul(a, b), M.r2); }
     __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const {
         const uint32_t d = a - b;
@@ -85,7 +96,10 @@ struct ArithMont {  // odd p >= 2^31
     Mont32 M;
     __device__ ArithMont(const decltype(CandArgs::M)& c) : M(c) {}
     __device__ __forceinline__ uint32_t prep(uint32_t v) const { return M.to_mont(v); }
-    __device__ __forceinline__ uint32_t mulp(uint32_t f, uint32_t vp) const { return M.montmul(f, vp); }
+    __device__ __forceinline__ uint32_t aux(uint32_t) const { return 0u; }
+    __device__ __forceinline__ uint32_t mulsub(uint32_t x, uint32_t f, uint32_t vp, uint32_t) const {
+        return M.sub(x, M.montmul(f, vp));
+    }
     __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return M.montmul(M.to_mont(a), b); }
     __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
     __device__ __forceinline__ uint32_t inverse(uint32_t a) const { return cp_inverse<true>(M, a); }
@@ -94,7 +108,10 @@ struct ArithTwo {  // p = 2
     Mont32 M;
     __device__ ArithTwo(const decltype(CandArgs::M)& c) : M(c) {}
     __device__ __forceinline__ uint32_t prep(uint32_t v) const { return v; }
-    __device__ __forceinline__ uint32_t mulp(uint32_t f, uint32_t vp) const { return M.barrett((uint64_t)f * vp); }
+    __device__ __forceinline__ uint32_t aux(uint32_t) const { return 0u; }
+    __device__ __forceinline__ uint32_t mulsub(uint32_t x, uint32_t f, uint32_t vp, uint32_t) const {
+        return M.sub(x, M.barrett((uint64_t)f * vp));
+    }
     __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return M.barrett((uint64_t)a * b); }
     __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
     __device__ __forceinline__ uint32_t inverse(uint32_t) const { return 1u; }
@@ -134,6 +151,7 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
     uint32_t* tile = (uint32_t*)smem_raw;                 // [bw][LDT]
     uint32_t* nprM = tile + (size_t)LDT * kMaxPanel;      // [kMaxPanel]
     uint32_t* fcol = nprM + kMaxPanel;                    // [256]
+    uint32_t* nprS = fcol + 256;                          // [kMaxPanel] aux(v) of the pivot row
     __shared__ int s_cand[256];
     __shared__ uint8_t s_isp[256];
     __shared__ int s_pr[kMaxPanel], s_pc[kMaxPanel];
@@ -231,6 +249,7 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
             uint32_t* e = tile + (size_t)cc * LDT + pi;
             const uint32_t v = (cc == c) ? inv : ar.mul(*e, inv);
             nprM[cc] = ar.prep(v);
+            nprS[cc] = ar.aux(v);
             *e = v;
         }
         for (int i = tid; i < n; i += blockDim.x) fcol[i] = (i == pi) ? 0u : tile[(size_t)c * LDT + i];
@@ -245,11 +264,11 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
         if (warp == 0) {
             if (c + 1 < bw) {
                 uint32_t* colp = tile + (size_t)(c + 1) * LDT;
-                const uint32_t vp = nprM[c + 1];
+                const uint32_t vp = nprM[c + 1], vs = nprS[c + 1];
 #pragma unroll
                 for (int j = 0; j < RPL; ++j) {
                     const int i = lane + 32 * j;
-                    if (fr[j] != 0u) colp[i] = ar.sub(colp[i], ar.mulp(fr[j], vp));
+                    if (fr[j] != 0u) colp[i] = ar.mulsub(colp[i], fr[j], vp, vs);
                 }
                 __syncwarp();
                 pick_pivot(c + 1, pi);
@@ -263,14 +282,14 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
             for (int t = warp - 1; t < ntarget; t += NW - 1) {
                 const int cc = (t < nright) ? c + 2 + t : ((t - nright < k) ? s_pc[t - nright] : c);
                 uint32_t* colp = tile + (size_t)cc * LDT;
-                const uint32_t vp = nprM[cc];
+                const uint32_t vp = nprM[cc], vs = nprS[cc];
                 const bool zero_first = (cc == c);
 #pragma unroll
                 for (int j = 0; j < RPL; ++j) {
                     const int i = lane + 32 * j;
                     if (fr[j] != 0u) {
                         const uint32_t x = zero_first ? 0u : colp[i];
-                        colp[i] = ar.sub(x, ar.mulp(fr[j], vp));
+                        colp[i] = ar.mulsub(x, fr[j], vp, vs);
                     }
                 }
             }

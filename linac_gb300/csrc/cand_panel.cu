@@ -40,7 +40,7 @@ static int launch_cand_typed(const CandArgs& a, size_t smem, cudaStream_t s) {
 }
 
 int launch_cand_panel(const CandArgs& a, cudaStream_t s) {
-    const size_t smem = (size_t)(a.smax | 1) * kMaxPanel * 4 + kMaxPanel * 4 + 256 * 4;
+    const size_t smem = (size_t)(a.smax | 1) * kMaxPanel * 4 + 2 * kMaxPanel * 4 + 256 * 4;
     if (!(a.M.p & 1u)) return launch_cand_typed<ArithTwo>(a, smem, s);
     if (a.M.p < (1u << 31)) return launch_cand_typed<ArithSmall>(a, smem, s);
     return launch_cand_typed<ArithMont>(a, smem, s);

@@ -404,26 +404,44 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
                 }
             }
         } else {
-            for (int t = 0; t < ntiles; ++t) {
-                const int buf = t & 1;
+            // C's old values are loaded one tile ahead, so their memory latency overlaps the
+            // previous tile's combine instead of stalling the accumulator hand-back
+            auto tile_at = [&](int t, uint32_t*& crow, int& ncols, bool& vec) {
                 const int64_t col0 = (int64_t)(t0 + t) * BN + 16 * half;
-                uint32_t* crow = P.C + (row_ok ? row : 0) * P.ldc + col0;
-                const int ncols = (int)((P.N - col0) < 16 ? (P.N - col0) : 16);
-                const bool vec = row_ok && ncols == 16 && ((((uintptr_t)crow) & 15) == 0);
-                uint32_t old[16];
+                crow = P.C + (row_ok ? row : 0) * P.ldc + col0;
+                ncols = (int)((P.N - col0) < 16 ? (P.N - col0) : 16);
+                vec = row_ok && ncols == 16 && ((((uintptr_t)crow) & 15) == 0);
+            };
+            auto load_old = [&](int t, uint32_t (&o)[16]) {
+                uint32_t* crow;
+                int ncols;
+                bool vec;
+                tile_at(t, crow, ncols, vec);
                 if (P.overwrite) {
-    #pragma unroll
-                    for (int c = 0; c < 16; ++c) old[c] = 0u;
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) o[c] = 0u;
                 } else if (vec) {
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 16; c += 4) {
                         const uint4 v = *(const uint4*)(crow + c);
-                        old[c] = v.x; old[c + 1] = v.y; old[c + 2] = v.z; old[c + 3] = v.w;
+                        o[c] = v.x; o[c + 1] = v.y; o[c + 2] = v.z; o[c + 3] = v.w;
                     }
                 } else {
-    #pragma unroll
-                    for (int c = 0; c < 16; ++c) old[c] = (row_ok && c < ncols) ? crow[c] : 0u;
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) o[c] = (row_ok && c < ncols) ? crow[c] : 0u;
                 }
+            };
+            uint32_t oldn[16];
+            if (ntiles > 0) load_old(0, oldn);
+            for (int t = 0; t < ntiles; ++t) {
+                const int buf = t & 1;
+                uint32_t* crow;
+                int ncols;
+                bool vec;
+                tile_at(t, crow, ncols, vec);
+                uint32_t old[16];
+#pragma unroll
+                for (int c = 0; c < 16; ++c) old[c] = oldn[c];
                 const bool got = ptx::mbar_wait(&acc_full[buf], (t >> 1) & 1, &s_err);
                 if (!__all_sync(0xffffffffu, got)) {  // warp-uniform before the aligned TMEM loads
                     if (lane == 0) flag_error(P, &s_err);
@@ -431,56 +449,56 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
                 }
                 ptx::tc_fence_after();
                 uint32_t d[GROUPS][16];
-    #pragma unroll
+#pragma unroll
                 for (int g = 0; g < GROUPS; ++g) ptx::tmem_ld16(t_lane + ACC_STRIDE * buf + BN * g, d[g]);
                 ptx::tmem_ld_wait();
                 // accumulator drained: re-zero it and hand it back to the MMA warp
-    #pragma unroll
+#pragma unroll
                 for (int g = 0; g < GROUPS; ++g) ptx::tmem_st16_zero(t_lane + ACC_STRIDE * buf + BN * g);
                 ptx::tmem_st_wait();
                 ptx::tc_fence_before();
                 __syncwarp();
                 if (lane == 0) ptx::mbar_arrive(&acc_empty[buf]);
+                if (t + 1 < ntiles) load_old(t + 1, oldn);
                 // exact conversion: for |x| <= 2^22, x + 1.5 * 2^23 is exact and its bit pattern minus
                 // 0x4B400000 is x (full-rate FADD instead of the quarter-rate F2I).  Groups 0, 1, 5, 6 hold
                 // at most two digit products per step and stay within 2^22 for any input; groups 2-4 are
                 // checked.  The weighted sum is formed modulo 2^64; its true value lies in [0, 2^60].
                 float mx = 0.f;
-    #pragma unroll
+#pragma unroll
                 for (int g = 2; g <= 4; ++g)
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
                 const bool fast = mx <= 4194304.0f;
-                uint32_t res[16];
                 if (__all_sync(0xffffffffu, fast)) {
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 16; ++c) {
                         uint64_t v = (uint64_t)bias;
-    #pragma unroll
+#pragma unroll
                         for (int g = 0; g < GROUPS; ++g) {
                             const int32_t y = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F));
                             v += (uint64_t)((int64_t)y * (int64_t)w[g]);
                         }
-                        res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
+                        old[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
                     }
                 } else {
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 16; ++c) {
                         uint64_t v = P.off;
-    #pragma unroll
+#pragma unroll
                         for (int g = 0; g < GROUPS; ++g)
                             v += (uint64_t)((int64_t)__float2int_rn(__uint_as_float(d[g][c])) * (int64_t)w[g]);
-                        res[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
+                        old[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
                     }
                 }
                 if (vec) {
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 16; c += 4)
-                        *(uint4*)(crow + c) = make_uint4(res[c], res[c + 1], res[c + 2], res[c + 3]);
+                        *(uint4*)(crow + c) = make_uint4(old[c], old[c + 1], old[c + 2], old[c + 3]);
                 } else if (row_ok) {
-    #pragma unroll
+#pragma unroll
                     for (int c = 0; c < 16; ++c)
-                        if (c < ncols) crow[c] = res[c];
+                        if (c < ncols) crow[c] = old[c];
                 }
             }
         }

@@ -200,8 +200,8 @@ static __global__ void __launch_bounds__(THREADS, 1)
         // ------------------------------------------------------------ MMA issuer
         if (lane == 0) {
             constexpr uint32_t idesc = ptx::umma_idesc_bf16(BM, B_ROWS);
-            const uint32_t a_base = ptx::smem_u32(sA);
-            const uint32_t b_base = ptx::smem_u32(sB);
+            const uint64_t adesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sA));  // K steps move the address field
+            const uint64_t bdesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sB));
             bool ok = ptx::mbar_wait(a_full, 0, &s_err);
             if (!ok) flag_error64(P, &s_err);
             const int ksteps = (k + 15) / 16;  // K steps beyond k are all zero (and skipped)
@@ -213,10 +213,10 @@ static __global__ void __launch_bounds__(THREADS, 1)
                 ptx::tc_fence_after();
                 const uint32_t dbase = tmem + ACC_STRIDE * buf;
                 for (int ks = 0; ks < ksteps; ++ks) {
-                    const uint64_t bdesc = ptx::umma_desc_sw128(b_base + st * B_TILE_BYTES + ks * 32);
+                    const uint64_t bdesc = bdesc0 + (uint64_t)((st * B_TILE_BYTES + ks * 32) >> 4);
 #pragma unroll
                     for (int i = 0; i < LIMBS; ++i) {
-                        const uint64_t adesc = ptx::umma_desc_sw128(a_base + i * A_TILE_BYTES + ks * 32);
+                        const uint64_t adesc = adesc0 + (uint64_t)((i * A_TILE_BYTES + ks * 32) >> 4);
                         ptx::umma_bf16(dbase + (uint32_t)(BN * i), adesc, bdesc, idesc, 1u);
                     }
                 }

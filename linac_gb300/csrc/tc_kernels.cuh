@@ -289,8 +289,10 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
         // ------------------------------------------------------------ MMA issuer
         if (lane == 0) {
             constexpr uint32_t idesc = ptx::umma_idesc_bf16(BM, B_ROWS);
-            const uint32_t a_base = ptx::smem_u32(sA);
-            const uint32_t b_base = ptx::smem_u32(sB);
+            // descriptors of the ring / plane bases; a K step or a stage moves only the start-address
+            // field (address / 16, 14 bits: shared-memory offsets never carry out of it)
+            const uint64_t adesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sA));
+            const uint64_t bdesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sB));
             bool ok = ptx::mbar_wait(a_full, 0, &s_err);
             if (!ok) flag_error(P, &s_err);
             int it = 0;
@@ -305,11 +307,11 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
                     ptx::tc_fence_after();
 #pragma unroll
                     for (int ks = 0; ks < KC / 16; ++ks) {
-                        const uint64_t bdesc = ptx::umma_desc_sw128(b_base + st * B_TILE_BYTES + ks * 32);
+                        const uint64_t bdesc = bdesc0 + (uint64_t)((st * B_TILE_BYTES + ks * 32) >> 4);
 #pragma unroll
                         for (int i = 0; i < LIMBS; ++i) {
                             const uint64_t adesc =
-                                ptx::umma_desc_sw128(a_base + (i * NKC + kc) * A_TILE_BYTES + ks * 32);
+                                adesc0 + (uint64_t)(((i * NKC + kc) * A_TILE_BYTES + ks * 32) >> 4);
                             ptx::umma_bf16(dbase + (uint32_t)(BN * i), adesc, bdesc, idesc, 1u);
                         }
                     }

@@ -70,6 +70,16 @@ __device__ __forceinline__ bool better(K ka, int64_t ra, K kb, int64_t rb) {
 
 template <class T>
 __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
+
+// a value of lane `src` of the warp, for the field element types
+__device__ __forceinline__ uint32_t shfl_value(uint32_t v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ uint64_t shfl_value(uint64_t v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double shfl_value(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ c128 shfl_value(c128 v, int src) {
+    v.x = __shfl_sync(0xffffffffu, v.x, src);
+    v.y = __shfl_sync(0xffffffffu, v.y, src);
+    return v;
+}
 template <>
 __device__ __forceinline__ c128 ldcg<c128>(const c128* p) {
     double2 v = __ldcg((const double2*)p);
@@ -144,12 +154,8 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_kernel(PanelArgs<F> a)
     __shared__ int s_pcols[kMaxPanel];
     __shared__ Key s_wkey[NW];
     __shared__ int64_t s_wrow[NW];
-    __shared__ int s_wblk[NW];
-    __shared__ int64_t s_cand_row;
     __shared__ int64_t s_win_row;
-    __shared__ int s_win_blk;
     __shared__ int s_win_ok;
-    __shared__ T s_inv;
 
     if (ld_volatile_i32(a.bar.err) != 0) return;
     if (a.run_if != nullptr && ld_volatile_i32(a.run_if) == 0) {
@@ -170,12 +176,15 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_kernel(PanelArgs<F> a)
     for (int c = 0; c < bw; ++c) {
         if (rank0 + k >= a.m) break;  // every row is a pivot row already
         const int par = c & 1;
-        // -- local proposal: best eligible row of this CTA for column c
+        // -- local proposal: best eligible row of this CTA for column c (warps reduce their rows,
+        //    warp 0 combines the warps and publishes the candidate row); own rows' column c to fcol
         Key bk = KeyNone<F>::v();
         int64_t br = INT64_MAX;
         for (int r = threadIdx.x; r < R; r += blockDim.x) {
+            const T v = tile[(size_t)r * bw + c];
+            fcol[r] = v;
             if (!used[r]) {
-                Key kk = f.key(tile[(size_t)r * bw + c]);
+                Key kk = f.key(v);
                 if (better(kk, r0 + r, bk, br)) { bk = kk; br = r0 + r; }
             }
         }
@@ -186,71 +195,85 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_kernel(PanelArgs<F> a)
         }
         if (lane == 0) { s_wkey[warp] = bk; s_wrow[warp] = br; }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int w = 1; w < NW; ++w)
-                if (better(s_wkey[w], s_wrow[w], bk, br)) { bk = s_wkey[w]; br = s_wrow[w]; }
-            a.cand_key[par * G + blockIdx.x] = bk;
-            a.cand_row[par * G + blockIdx.x] = br;
-            s_cand_row = br;
-        }
-        __syncthreads();
-        if (s_cand_row != INT64_MAX) {
-            const int rl = (int)(s_cand_row - r0);
-            T* dst = a.cand_vals + ((size_t)par * G + blockIdx.x) * a.b;
-            for (int cc = threadIdx.x; cc < bw; cc += blockDim.x) dst[cc] = tile[(size_t)rl * bw + cc];
+        if (warp == 0) {
+            bk = (lane < NW) ? s_wkey[lane] : KeyNone<F>::v();
+            br = (lane < NW) ? s_wrow[lane] : INT64_MAX;
+            for (int o = 16; o; o >>= 1) {
+                Key ok = __shfl_xor_sync(0xffffffffu, bk, o);
+                int64_t orow = __shfl_xor_sync(0xffffffffu, br, o);
+                if (better(ok, orow, bk, br)) { bk = ok; br = orow; }
+            }
+            if (lane == 0) {
+                a.cand_key[par * G + blockIdx.x] = bk;
+                a.cand_row[par * G + blockIdx.x] = br;
+            }
+            if (br != INT64_MAX) {
+                const int rl = (int)(br - r0);
+                T* dst = a.cand_vals + ((size_t)par * G + blockIdx.x) * a.b;
+                for (int cc = lane; cc < bw; cc += 32) dst[cc] = tile[(size_t)rl * bw + cc];
+            }
         }
         // -- exchange
         if (!grid_sync(a.bar)) return;
-        // -- winner over all CTAs (identical in every CTA)
-        {
+        // -- winner over all CTAs (warp 0; identical in every CTA) and its row, normalised, in prow
+        if (warp == 0) {
             Key wk = KeyNone<F>::v();
             int64_t wr = INT64_MAX;
             int wb = -1;
-            for (int g = threadIdx.x; g < G; g += blockDim.x) {
-                int64_t rr = ldcg(a.cand_row + par * G + g);
-                if (rr != INT64_MAX) {
-                    Key kk = ldcg(a.cand_key + par * G + g);
-                    if (better(kk, rr, wk, wr)) { wk = kk; wr = rr; wb = g; }
-                }
+            // all proposals in one round of independent loads (G <= 32 * GL CTAs)
+            constexpr int GL = 8;
+            int64_t rrs[GL];
+            Key kks[GL];
+#pragma unroll
+            for (int j = 0; j < GL; ++j) {
+                const int g = lane + 32 * j;
+                rrs[j] = (g < G) ? ldcg(a.cand_row + par * G + g) : INT64_MAX;
+                kks[j] = (g < G) ? ldcg(a.cand_key + par * G + g) : KeyNone<F>::v();
             }
+#pragma unroll
+            for (int j = 0; j < GL; ++j)
+                if (rrs[j] != INT64_MAX && better(kks[j], rrs[j], wk, wr)) { wk = kks[j]; wr = rrs[j]; wb = lane + 32 * j; }
             for (int o = 16; o; o >>= 1) {
-                Key ok = __shfl_down_sync(0xffffffffu, wk, o);
-                int64_t orow = __shfl_down_sync(0xffffffffu, wr, o);
-                int ob = __shfl_down_sync(0xffffffffu, wb, o);
+                Key ok = __shfl_xor_sync(0xffffffffu, wk, o);
+                int64_t orow = __shfl_xor_sync(0xffffffffu, wr, o);
+                int ob = __shfl_xor_sync(0xffffffffu, wb, o);
                 if (better(ok, orow, wk, wr)) { wk = ok; wr = orow; wb = ob; }
             }
-            if (lane == 0) { s_wkey[warp] = wk; s_wrow[warp] = wr; s_wblk[warp] = wb; }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                for (int w = 1; w < NW; ++w)
-                    if (better(s_wkey[w], s_wrow[w], wk, wr)) { wk = s_wkey[w]; wr = s_wrow[w]; wb = s_wblk[w]; }
+            const bool ok = (wr != INT64_MAX) && f.is_pivot(wk);
+            if (ok) {
+                // the winner's row in one round of loads (kMaxPanel / 32 per lane), its pivot
+                // from the lane holding column c, the inverse in every lane
+                const T* src = a.cand_vals + ((size_t)par * G + wb) * a.b;
+                constexpr int PL = kMaxPanel / 32;
+                T v[PL];
+#pragma unroll
+                for (int j = 0; j < PL; ++j) {
+                    const int cc = lane + 32 * j;
+                    v[j] = (cc < bw) ? ldcg(src + cc) : f.zero();
+                }
+                T piv = f.zero();
+#pragma unroll
+                for (int j = 0; j < PL; ++j)
+                    if (j == (c >> 5)) piv = v[j];
+                piv = shfl_value(piv, c & 31);
+                const T pinv = f.inv(piv);
+#pragma unroll
+                for (int j = 0; j < PL; ++j) {
+                    const int cc = lane + 32 * j;
+                    if (cc < bw) prow[cc] = (cc == c) ? pinv : f.scale(v[j], piv, pinv);
+                }
+            }
+            if (lane == 0) {
                 s_win_row = wr;
-                s_win_blk = wb;
-                s_win_ok = (wr != INT64_MAX) && f.is_pivot(wk);
+                s_win_ok = ok ? 1 : 0;
                 if constexpr (F::kDtype >= 3) {
                     if (a.uncertain && wr != INT64_MAX && wk > a.band_lo && wk <= a.band_hi) atomicExch(a.uncertain, 1);
                 }
             }
-            __syncthreads();
         }
+        __syncthreads();
         if (!s_win_ok) continue;  // column c has no pivot (uniform decision)
         const int64_t wrow = s_win_row;
-        {
-            const T* src = a.cand_vals + ((size_t)par * G + s_win_blk) * a.b;
-            for (int cc = threadIdx.x; cc < bw; cc += blockDim.x) prow[cc] = ldcg(src + cc);
-            for (int r = threadIdx.x; r < R; r += blockDim.x) fcol[r] = tile[(size_t)r * bw + c];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) s_inv = f.inv(prow[c]);
-        __syncthreads();
-        {
-            const T piv = prow[c];
-            const T pinv = s_inv;
-            __syncthreads();
-            for (int cc = threadIdx.x; cc < bw; cc += blockDim.x)
-                prow[cc] = (cc == c) ? pinv : f.scale(prow[cc], piv, pinv);
-        }
-        __syncthreads();
         // -- eliminate own rows (Gauss-Jordan, above and below), keeping the
         //    transform in column c
         for (int r = warp; r < R; r += NW) {

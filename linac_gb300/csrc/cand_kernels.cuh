@@ -34,22 +34,6 @@ struct Mont32 {
     __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return a >= b ? a - b : a + (p - b); }
 };
 
-template <bool MONT>
-__device__ __forceinline__ uint32_t cp_inverse(const Mont32& M, uint32_t a) {
-    if constexpr (MONT) {
-        uint32_t x = M.to_mont(a), r = M.to_mont(1u);
-        uint64_t e = (uint64_t)M.p - 2;
-        while (e) {
-            if (e & 1) r = M.montmul(r, x);
-            x = M.montmul(x, x);
-            e >>= 1;
-        }
-        return M.from_mont(r);
-    } else {
-        return 1u;  // p = 2: the only non-zero residue is its own inverse
-    }
-}
-
 // Arithmetic policies of the candidate panel.  `prep` / `aux` turn a
 // normalised pivot-row value v into the form(s) the update uses, and
 // `mulsub(x, f, prep(v), aux(v))` is x - f v mod p; `mul` multiplies two
@@ -81,16 +65,7 @@ struct ArithSmall {  // odd p < 2^31: 32-bit Montgomery, reductions by unsigned 
         const uint32_t d = a - b;
         return min(d, d + M.p);
     }
-    __device__ __forceinline__ uint32_t inverse(uint32_t a) const {
-        uint32_t x = montmul(a, M.r2), r = montmul(1u, M.r2);
-        uint32_t e = M.p - 2;
-        while (e) {
-            if (e & 1u) r = montmul(r, x);
-            x = montmul(x, x);
-            e >>= 1;
-        }
-        return red((uint64_t)r);
-    }
+    __device__ __forceinline__ uint32_t inverse(uint32_t a) const { return inv_binary<uint32_t>(a, M.p); }
 };
 struct ArithMont {  // odd p >= 2^31
     Mont32 M;
@@ -102,7 +77,7 @@ struct ArithMont {  // odd p >= 2^31
     }
     __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return M.montmul(M.to_mont(a), b); }
     __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
-    __device__ __forceinline__ uint32_t inverse(uint32_t a) const { return cp_inverse<true>(M, a); }
+    __device__ __forceinline__ uint32_t inverse(uint32_t a) const { return inv_binary<uint32_t>(a, M.p); }
 };
 struct ArithTwo {  // p = 2
     Mont32 M;
@@ -116,6 +91,24 @@ struct ArithTwo {  // p = 2
     __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
     __device__ __forceinline__ uint32_t inverse(uint32_t) const { return 1u; }
 };
+
+struct Arith64 {  // 64-bit residues (odd p < 2^64): Montgomery with R = 2^64
+    FieldU64 F;
+    __device__ Arith64(const CandArgs& a) : F(a.f64) {}
+    __device__ __forceinline__ uint64_t prep(uint64_t v) const { return F.to_mont(v); }
+    __device__ __forceinline__ uint64_t aux(uint64_t) const { return 0ull; }
+    __device__ __forceinline__ uint64_t mulsub(uint64_t x, uint64_t f, uint64_t vp, uint64_t) const {
+        return F.sub(x, F.montmul(f, vp));  // f (v R) R^-1 = f v
+    }
+    __device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) const { return F.mul(a, b); }
+    __device__ __forceinline__ uint64_t inverse(uint64_t a) const { return inv_binary<uint64_t>(a, F.p); }
+};
+
+// arithmetic policies are built from the panel arguments
+template <class Arith>
+__device__ __forceinline__ Arith make_arith(const CandArgs& a) { return Arith(a.M); }
+template <>
+__device__ __forceinline__ Arith64 make_arith<Arith64>(const CandArgs& a) { return Arith64(a); }
 
 // block-wide exclusive scan of a 0/1 flag (blockDim.x <= 1024); returns the
 // prefix, writes the total to *total (shared)
@@ -141,25 +134,32 @@ __device__ __forceinline__ int block_scan_flag(int flag, int* s_warp, int* total
     return r;
 }
 
-template <class Arith>
+// dynamic shared memory of the candidate panel for word type W and panel width PW
+template <class W, int PW>
+__host__ __device__ constexpr size_t cand_smem(int smax) {
+    return ((size_t)(smax | 1) * PW + 2 * PW + 256) * sizeof(W);
+}
+
+// W: residue word (uint32_t, or uint64_t for 64-bit primes); PW: panel width
+template <class Arith, class W = uint32_t, int PW = kMaxPanel>
 __device__ __forceinline__ void cand_body(const CandArgs& a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int bw = a.bw;
     // column-major block, odd pitch: a column (fixed c, consecutive rows) and a
     // row (fixed i, consecutive columns) are both free of bank conflicts
     const int LDT = a.smax | 1;
-    uint32_t* tile = (uint32_t*)smem_raw;                 // [bw][LDT]
-    uint32_t* nprM = tile + (size_t)LDT * kMaxPanel;      // [kMaxPanel]
-    uint32_t* fcol = nprM + kMaxPanel;                    // [256]
-    uint32_t* nprS = fcol + 256;                          // [kMaxPanel] aux(v) of the pivot row
+    W* tile = (W*)smem_raw;                   // [bw][LDT]
+    W* nprM = tile + (size_t)LDT * PW;        // [PW]
+    W* fcol = nprM + PW;                      // [256]
+    W* nprS = fcol + 256;                     // [PW] aux(v) of the pivot row
     __shared__ int s_cand[256];
     __shared__ uint8_t s_isp[256];
-    __shared__ int s_pr[kMaxPanel], s_pc[kMaxPanel];
+    __shared__ int s_pr[PW], s_pc[PW];
     __shared__ int s_warp[32];
     __shared__ int s_n, s_total, s_next;
     __shared__ int s_npi;           // look-ahead: pivot row of the next column (-1: none)
-    __shared__ uint32_t s_ninv;     // and the inverse of its entry
-    const Arith ar(a.M);
+    __shared__ W s_ninv;            // and the inverse of its entry
+    const Arith ar = make_arith<Arith>(a);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     constexpr int NW = kCandThreads / 32;
 
@@ -202,7 +202,7 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
     const int n = s_n;
     // ---- load the candidate block
     for (int i = warp; i < n; i += NW) {
-        const uint32_t* src = a.A + (int64_t)s_cand[i] * a.lda + a.j0;
+        const W* src = (const W*)a.A + (int64_t)s_cand[i] * a.lda + a.j0;
         for (int c = lane; c < bw; c += 32) tile[(size_t)c * LDT + i] = src[c];
     }
     for (int i = tid; i < 256; i += blockDim.x) s_isp[i] = 0;
@@ -218,16 +218,16 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
         // warp 0: first candidate row, not a pivot row and not `exclude`, with a
         // non-zero entry in column `col`; lane 0 then computes its inverse
         int found = -1;
-        const uint32_t* colp = tile + (size_t)col * LDT;
+        const W* colp = tile + (size_t)col * LDT;
         for (int base = 0; base < n && found < 0; base += 32) {
             const int i = base + lane;
-            const bool ok = i < n && !s_isp[i] && i != exclude && colp[i] != 0u;
+            const bool ok = i < n && !s_isp[i] && i != exclude && colp[i] != 0;
             const unsigned b = __ballot_sync(0xffffffffu, ok);
             if (b) found = base + __ffs(b) - 1;
         }
         if (lane == 0) {
             s_npi = found;
-            s_ninv = (found >= 0) ? ar.inverse(colp[found]) : 0u;
+            s_ninv = (found >= 0) ? ar.inverse(colp[found]) : (W)0;
         }
     };
     if (warp == 0) pick_pivot(0, -1);
@@ -235,7 +235,7 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
     int k = 0;
     for (int c = 0; c < bw; ++c) {
         const int pi = s_npi;
-        const uint32_t inv = s_ninv;
+        const W inv = s_ninv;
         if (pi < 0) {
             // column c has no pivot: nothing changes, look at column c + 1
             __syncthreads();
@@ -246,29 +246,29 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
         // normalised pivot row (its column c holds the inverse: the transform) and
         // the multipliers of every other row
         for (int cc = tid; cc < bw; cc += blockDim.x) {
-            uint32_t* e = tile + (size_t)cc * LDT + pi;
-            const uint32_t v = (cc == c) ? inv : ar.mul(*e, inv);
+            W* e = tile + (size_t)cc * LDT + pi;
+            const W v = (cc == c) ? inv : ar.mul(*e, inv);
             nprM[cc] = ar.prep(v);
             nprS[cc] = ar.aux(v);
             *e = v;
         }
-        for (int i = tid; i < n; i += blockDim.x) fcol[i] = (i == pi) ? 0u : tile[(size_t)c * LDT + i];
+        for (int i = tid; i < n; i += blockDim.x) fcol[i] = (i == pi) ? (W)0 : tile[(size_t)c * LDT + i];
         __syncthreads();
         // this lane's rows and their multipliers (0 for the pivot row and absent rows)
-        uint32_t fr[RPL];
+        W fr[RPL];
 #pragma unroll
         for (int j = 0; j < RPL; ++j) {
             const int i = lane + 32 * j;
-            fr[j] = (i < n) ? fcol[i] : 0u;
+            fr[j] = (i < n) ? fcol[i] : (W)0;
         }
         if (warp == 0) {
             if (c + 1 < bw) {
-                uint32_t* colp = tile + (size_t)(c + 1) * LDT;
-                const uint32_t vp = nprM[c + 1], vs = nprS[c + 1];
+                W* colp = tile + (size_t)(c + 1) * LDT;
+                const W vp = nprM[c + 1], vs = nprS[c + 1];
 #pragma unroll
                 for (int j = 0; j < RPL; ++j) {
                     const int i = lane + 32 * j;
-                    if (fr[j] != 0u) colp[i] = ar.mulsub(colp[i], fr[j], vp, vs);
+                    if (fr[j] != 0) colp[i] = ar.mulsub(colp[i], fr[j], vp, vs);
                 }
                 __syncwarp();
                 pick_pivot(c + 1, pi);
@@ -281,14 +281,14 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
             const int ntarget = nright + k + 1;
             for (int t = warp - 1; t < ntarget; t += NW - 1) {
                 const int cc = (t < nright) ? c + 2 + t : ((t - nright < k) ? s_pc[t - nright] : c);
-                uint32_t* colp = tile + (size_t)cc * LDT;
-                const uint32_t vp = nprM[cc], vs = nprS[cc];
+                W* colp = tile + (size_t)cc * LDT;
+                const W vp = nprM[cc], vs = nprS[cc];
                 const bool zero_first = (cc == c);
 #pragma unroll
                 for (int j = 0; j < RPL; ++j) {
                     const int i = lane + 32 * j;
-                    if (fr[j] != 0u) {
-                        const uint32_t x = zero_first ? 0u : colp[i];
+                    if (fr[j] != 0) {
+                        const W x = zero_first ? (W)0 : colp[i];
                         colp[i] = ar.mulsub(x, fr[j], vp, vs);
                     }
                 }
@@ -306,9 +306,10 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
 
     // ---- outputs
     const int64_t rank0 = *a.rank;
-    for (int idx = tid; idx < kMaxPanel * kMaxPanel; idx += blockDim.x) {
-        const int t = idx / kMaxPanel, u = idx % kMaxPanel;
-        a.X[idx] = (t < k && u < k) ? tile[(size_t)s_pc[u] * LDT + s_pr[t]] : 0u;
+    W* X = (W*)a.X;  // [PW][PW]
+    for (int idx = tid; idx < PW * PW; idx += blockDim.x) {
+        const int t = idx / PW, u = idx % PW;
+        X[idx] = (t < k && u < k) ? tile[(size_t)s_pc[u] * LDT + s_pr[t]] : (W)0;
     }
     for (int t = tid; t < k; t += blockDim.x) {
         const int r = s_cand[s_pr[t]];
@@ -338,9 +339,9 @@ __device__ __forceinline__ void cand_body(const CandArgs& a) {
     }
 }
 
-template <class Arith>
+template <class Arith, class W = uint32_t, int PW = kMaxPanel>
 static __global__ void __launch_bounds__(kCandThreads, 1) cand_panel_kernel(const __grid_constant__ CandArgs a) {
-    cand_body<Arith>(a);
+    cand_body<Arith, W, PW>(a);
 }
 
 // G operand of E = G X, as four K-major digit planes: G[o, t] = -A[o, j0 + c_t]
@@ -386,7 +387,8 @@ __device__ __forceinline__ void split_g_body(const uint32_t* A, int64_t lda, int
 // After the update every remaining (non-pivot) row must be zero in the
 // panel's non-pivot columns; a non-zero entry means the candidate block missed
 // a pivot.
-__device__ __forceinline__ void check_missed_body(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, int bw,
+template <class W = uint32_t>
+__device__ __forceinline__ void check_missed_body(const W* A, int64_t lda, int64_t m, int64_t j0, int bw,
                                                   const uint8_t* row_used, const uint32_t* pivmask, int* missed) {
     __shared__ uint32_t s_mask[4];
     if (threadIdx.x < 4) s_mask[threadIdx.x] = pivmask[threadIdx.x];
@@ -397,9 +399,9 @@ __device__ __forceinline__ void check_missed_body(const uint32_t* A, int64_t lda
     int bad = 0;
     for (int64_t r = wid; r < m; r += nw) {
         if (row_used[r]) continue;
-        const uint32_t* row = A + r * lda + j0;
+        const W* row = A + r * lda + j0;
         for (int c = lane; c < bw; c += 32)
-            if (!((s_mask[c >> 5] >> (c & 31)) & 1u) && row[c] != 0u) bad = 1;
+            if (!((s_mask[c >> 5] >> (c & 31)) & 1u) && row[c] != 0) bad = 1;
     }
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(missed, 1);
 }
@@ -410,9 +412,10 @@ static __global__ void split_g_kernel(const uint32_t* A, int64_t lda, int64_t m,
     split_g_body(A, lda, m, m_pad, j0, p, panel_k, panel_cols, panel_mark, gen, EL);
 }
 
-static __global__ void check_missed_kernel(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, int bw,
+template <class W = uint32_t>
+static __global__ void check_missed_kernel(const W* A, int64_t lda, int64_t m, int64_t j0, int bw,
                                            const uint8_t* row_used, const uint32_t* pivmask, int* missed) {
-    check_missed_body(A, lda, m, j0, bw, row_used, pivmask, missed);
+    check_missed_body<W>(A, lda, m, j0, bw, row_used, pivmask, missed);
 }
 
 }  // namespace lnc

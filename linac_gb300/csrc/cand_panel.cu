@@ -46,6 +46,25 @@ int launch_cand_panel(const CandArgs& a, cudaStream_t s) {
     return launch_cand_typed<ArithMont>(a, smem, s);
 }
 
+int launch_cand_panel64(const CandArgs& a, cudaStream_t s) {
+    const size_t smem = cand_smem<uint64_t, kPanelU64>(a.smax);
+    auto kern = cand_panel_kernel<Arith64, uint64_t, kPanelU64>;
+    LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ScopedKernelTimer kt(KC_PANEL, s, 2.0 * a.smax * a.bw * 8.0);
+    kern<<<1, kCandThreads, smem, s>>>(a);
+    LNC_CHECK_LAUNCH("cand_panel_kernel (64-bit)");
+    return LNC_OK;
+}
+
+int launch_check_missed64(const uint64_t* A, int64_t lda, int64_t m, int64_t j0, int bw, const uint8_t* row_used,
+                          const uint32_t* pivmask, int* missed, cudaStream_t s) {
+    const int64_t warps = std::min<int64_t>(m, 152 * 64);
+    const int grid = (int)std::max<int64_t>(1, (warps * 32 + 255) / 256);
+    check_missed_kernel<uint64_t><<<grid, 256, 0, s>>>(A, lda, m, j0, bw, row_used, pivmask, missed);
+    LNC_CHECK_LAUNCH("check_missed_kernel (64-bit)");
+    return LNC_OK;
+}
+
 int launch_split_g(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, uint32_t p, const int32_t* panel_k,
                    const int32_t* panel_cols, const int32_t* panel_mark, int gen, void* EL, cudaStream_t s) {
     const int m_pad = tc_m_pad(m);

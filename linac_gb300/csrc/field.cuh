@@ -31,6 +31,36 @@ struct c128 {
 // ----------------------------------------------------------------------------
 // F_p, 32-bit residues
 // ----------------------------------------------------------------------------
+// Multiplicative inverse of a (0 < a < p, p prime) by the binary extended
+// Euclidean algorithm: invariants x1 a = u, x2 a = v (mod p); halving x mod p
+// is x / 2 or (x + p) / 2 = x/2 + p/2 + 1 for odd x (no overflow for any
+// p < 2^64).  About 2 log2(p) short dependent steps, several times shorter
+// than Fermat's log2(p) modular squarings on the pivot's critical path.
+template <class W>
+__device__ __forceinline__ W inv_binary(W a, W p) {
+    if (a == 1) return 1;  // also the only case for p = 2
+    W u = a, v = p, x1 = 1, x2 = 0;
+    const W half = (p >> 1) + 1;
+    while (u != 1 && v != 1) {
+        while (!(u & 1)) {
+            u >>= 1;
+            x1 = (x1 & 1) ? (x1 >> 1) + half : (x1 >> 1);
+        }
+        while (!(v & 1)) {
+            v >>= 1;
+            x2 = (x2 & 1) ? (x2 >> 1) + half : (x2 >> 1);
+        }
+        if (u >= v) {
+            u -= v;
+            x1 = (x1 >= x2) ? x1 - x2 : x1 + (p - x2);
+        } else {
+            v -= u;
+            x2 = (x2 >= x1) ? x2 - x1 : x2 + (p - x1);
+        }
+    }
+    return (u == 1) ? x1 : x2;
+}
+
 struct FieldU32 {
     using T = uint32_t;
     using Key = uint64_t;
@@ -68,7 +98,7 @@ struct FieldU32 {
         }
         return r;
     }
-    __device__ __forceinline__ T inv(T a) const { return pow(a, (uint64_t)p - 2); }
+    __device__ __forceinline__ T inv(T a) const { return inv_binary<uint32_t>(a, p); }
     __device__ __forceinline__ T scale(T x, T /*piv*/, T pinv) const { return mul(x, pinv); }
     __device__ __forceinline__ Key key(T a) const { return (Key)a; }
     __device__ __forceinline__ bool is_pivot(Key k) const { return k != 0; }
@@ -122,17 +152,7 @@ struct FieldU64 {
     __device__ __forceinline__ T sub(T a, T b) const { return a >= b ? a - b : a + (p - b); }
     __device__ __forceinline__ T zero() const { return 0ull; }
     __device__ __forceinline__ T one() const { return 1ull; }
-    __device__ __forceinline__ T inv(T a) const {
-        // Fermat in the Montgomery domain: a^(p-2)
-        T x = to_mont(a), r = r1;
-        uint64_t e = p - 2;
-        while (e) {
-            if (e & 1) r = montmul(r, x);
-            x = montmul(x, x);
-            e >>= 1;
-        }
-        return from_mont(r);
-    }
+    __device__ __forceinline__ T inv(T a) const { return inv_binary<uint64_t>(a, p); }
     __device__ __forceinline__ T scale(T x, T /*piv*/, T pinv_) const { return mul(x, pinv_); }
     __device__ __forceinline__ Key key(T a) const { return a; }
     __device__ __forceinline__ bool is_pivot(Key k) const { return k != 0; }

@@ -573,7 +573,7 @@ size_t rref_scratch_bytes(int64_t m, int64_t n, const RrefPlan& pl) {
     s += align_up(sizeof(T) * (size_t)m * pl.b, 256);           // E
     s += align_up(sizeof(T) * (size_t)pl.b * (size_t)std::max<int64_t>(n, 1), 256);  // Bm
     s += trailing_extra_scratch<F>(m, n, pl);
-    if constexpr (F::kDtype == 1) s += fast_extra_scratch(m, n);
+    if constexpr (F::kDtype == 1 || F::kDtype == 2) s += fast_extra_scratch(m, n);
     return s;
 }
 
@@ -711,13 +711,19 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
         fast = !(flags & (LNC_FLAG_SIMT_TRAILING | LNC_FLAG_ROBUST_PANEL)) && pl.b == kMaxPanel &&
                trailing_tc_u32_available();
     }
+    if constexpr (F::kDtype == 2) {
+        fast = !(flags & (LNC_FLAG_SIMT_TRAILING | LNC_FLAG_ROBUST_PANEL)) && pl.b == kPanelU64 &&
+               trailing_tc_u64_available();
+    }
     if (fast) {
-        if constexpr (F::kDtype == 1) {
+        if constexpr (F::kDtype == 1 || F::kDtype == 2) {
+            constexpr bool U64 = F::kDtype == 2;
+            constexpr int PW = U64 ? kPanelU64 : kMaxPanel;  // panel width (contraction depth)
             // ---------------- candidate-block panels + tensor-core updates
             unsigned char* fx = (unsigned char*)extra + trailing_extra_scratch<F>(m, n, pl);
             fx = (unsigned char*)(((uintptr_t)fx + 255) & ~(uintptr_t)255);
             auto takef = [&](size_t bytes) { void* r = fx; fx += align_up(bytes, 256); return r; };
-            uint32_t* Xbuf = (uint32_t*)takef(sizeof(uint32_t) * kMaxPanel * kMaxPanel);
+            T* Xbuf = (T*)takef(sizeof(T) * PW * PW);
             int32_t* cand = (int32_t*)takef(sizeof(int32_t) * 256);
             unsigned char* fscal = (unsigned char*)takef(256);
             int32_t* cand_n = (int32_t*)fscal;
@@ -737,7 +743,7 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
             LNC_CUDA(cudaMemsetAsync(panel_mark, 0, sizeof(int32_t) * (size_t)m, s));
             unsigned char* tcb = (unsigned char*)(((uintptr_t)extra + 1023) & ~(uintptr_t)1023);
             void* EL = tcb;
-            void* BS = tcb + tc_el_bytes(m);
+            void* BS = U64 ? tc64_bs_base(extra, m) : (void*)(tcb + tc_el_bytes(m));
             CandArgs ca;
             ca.A = A;
             ca.lda = lda;
@@ -757,7 +763,9 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
             ca.X = Xbuf;
             ca.pivmask = pivmask;
             ca.missed = missed;
-            {
+            if constexpr (U64) {
+                ca.f64 = f;
+            } else {
                 const uint32_t pp = f.p;
                 uint32_t x = pp;
                 for (int i = 0; i < 5; ++i) x *= 2u - pp * x;
@@ -774,16 +782,32 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
                 ca.j0 = j0;
                 ca.bw = bw;
                 ca.gen = gen;
-                int rc = launch_cand_panel(ca, s);
-                if (!rc) rc = launch_split_g(A, lda, m, j0, f.p, panel_k, panel_cols, panel_mark, gen, EL, s);
-                // E = G X  (m x 128, overwritten)
-                if (!rc) rc = tc_gather_split_b(Xbuf, kMaxPanel, kMaxPanel, nullptr, panel_k, f.p, BS, false, s);
-                if (!rc) rc = tc_limb_gemm(f, E, kMaxPanel, m, kMaxPanel, panel_k, true, EL, BS, n, err, status, s);
-                // A[:, j0:] += E A[P, j0:]  (pivot rows zeroed first)
-                if (!rc) rc = tc_split_e(E, kMaxPanel, kMaxPanel, m, f.p, panel_k, EL, s);
-                if (!rc) rc = tc_gather_split_b(A + j0, lda, n - j0, panel_rows, panel_k, f.p, BS, true, s);
-                if (!rc) rc = tc_limb_gemm(f, A + j0, lda, m, n - j0, panel_k, false, EL, BS, n, err, status, s);
-                if (!rc) rc = launch_check_missed(A, lda, m, j0, bw, row_used, pivmask, defer ? missed_any : missed, s);
+                int* miss = defer ? missed_any : missed;
+                int rc = LNC_OK;
+                if constexpr (U64) {
+                    rc = launch_cand_panel64(ca, s);
+                    if (!rc) rc = tc64_split_g(A, lda, m, j0, f.p, panel_k, panel_cols, panel_mark, gen, EL, s);
+                    // E = G X  (m x 64, overwritten)
+                    if (!rc) rc = tc64_gather_split_b(Xbuf, PW, PW, nullptr, panel_k, f.p, BS, false, s);
+                    if (!rc) rc = tc64_limb_gemm(f, E, PW, m, PW, panel_k, true, EL, BS, err, status, s, true, PW);
+                    // A[:, j0:] += E A[P, j0:]  (pivot rows zeroed first)
+                    if (!rc) rc = tc64_split_e(E, PW, m, f.p, panel_k, EL, s);
+                    if (!rc) rc = tc64_gather_split_b(A + j0, lda, n - j0, panel_rows, panel_k, f.p, BS, true, s);
+                    if (!rc) rc = tc64_limb_gemm(f, A + j0, lda, m, n - j0, panel_k, false, EL, BS, err, status, s,
+                                                 true, PW);
+                    if (!rc) rc = launch_check_missed64(A, lda, m, j0, bw, row_used, pivmask, miss, s);
+                } else {
+                    rc = launch_cand_panel(ca, s);
+                    if (!rc) rc = launch_split_g(A, lda, m, j0, f.p, panel_k, panel_cols, panel_mark, gen, EL, s);
+                    // E = G X  (m x 128, overwritten)
+                    if (!rc) rc = tc_gather_split_b(Xbuf, kMaxPanel, kMaxPanel, nullptr, panel_k, f.p, BS, false, s);
+                    if (!rc) rc = tc_limb_gemm(f, E, kMaxPanel, m, kMaxPanel, panel_k, true, EL, BS, n, err, status, s);
+                    // A[:, j0:] += E A[P, j0:]  (pivot rows zeroed first)
+                    if (!rc) rc = tc_split_e(E, kMaxPanel, kMaxPanel, m, f.p, panel_k, EL, s);
+                    if (!rc) rc = tc_gather_split_b(A + j0, lda, n - j0, panel_rows, panel_k, f.p, BS, true, s);
+                    if (!rc) rc = tc_limb_gemm(f, A + j0, lda, m, n - j0, panel_k, false, EL, BS, n, err, status, s);
+                    if (!rc) rc = launch_check_missed(A, lda, m, j0, bw, row_used, pivmask, miss, s);
+                }
                 if (rc) return rc;
                 if (defer) continue;
                 // redo the panel exhaustively when the candidate block missed a pivot

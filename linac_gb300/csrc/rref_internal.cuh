@@ -173,7 +173,7 @@ struct CandMont {
     uint64_t mu;
 };
 struct CandArgs {
-    const uint32_t* A;
+    const void* A;        // residues (uint32, or uint64 for the 64-bit panel)
     int64_t lda;
     int64_t m;
     int64_t j0;
@@ -191,25 +191,41 @@ struct CandArgs {
     int32_t* panel_cols;
     int32_t* panel_mark;  // (gen << 8) | (t + 1) for the pivot rows of panel `gen`
     int gen;
-    uint32_t* X;          // [kMaxPanel][kMaxPanel] inverse of the pivot block
+    void* X;              // [PW][PW] inverse of the pivot block (residue words)
     uint32_t* pivmask;    // [4] pivot columns of the panel
     int* missed;
     struct {
         uint32_t p, pinv, r2;
         uint64_t mu;
     } M;
+    FieldU64 f64;         // 64-bit panel: the field's Montgomery constants
 };
 int launch_cand_panel(const CandArgs& a, cudaStream_t s);
 int launch_split_g(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, uint32_t p, const int32_t* panel_k,
                    const int32_t* panel_cols, const int32_t* panel_mark, int gen, void* EL, cudaStream_t s);
 int launch_check_missed(const uint32_t* A, int64_t lda, int64_t m, int64_t j0, int bw, const uint8_t* row_used,
                         const uint32_t* pivmask, int* missed, cudaStream_t s);
+// 64-bit residues: candidate panel of 64 columns and its miss check (cand_panel.cu)
+constexpr int kPanelU64 = 64;
+int launch_cand_panel64(const CandArgs& a, cudaStream_t s);
+int launch_check_missed64(const uint64_t* A, int64_t lda, int64_t m, int64_t j0, int bw, const uint8_t* row_used,
+                          const uint32_t* pivmask, int* missed, cudaStream_t s);
 
 // Tensor-core trailing update for 64-bit residues (trailing_tc64.cu); panels of <= 64 columns
 int trailing_update_tc_u64(const TrailingCtx<FieldU64>& t, cudaStream_t s);
 size_t trailing_tc_u64_scratch(int64_t m, int64_t n);
 bool trailing_tc_u64_available();
 constexpr int kMaxPanelU64Tc = 64;
+int tc64_split_e(const uint64_t* E, int64_t ldE, int64_t m, uint64_t p, const int32_t* k_ptr, void* EL,
+                 cudaStream_t s);
+int tc64_split_g(const uint64_t* A, int64_t lda, int64_t m, int64_t j0, uint64_t p, const int32_t* k_ptr,
+                 const int32_t* panel_cols, const int32_t* panel_mark, int gen, void* EL, cudaStream_t s);
+int tc64_gather_split_b(uint64_t* C, int64_t ldc, int64_t N, const int32_t* rows, const int32_t* k_ptr, uint64_t p,
+                        void* BS, bool zero_src, cudaStream_t s);
+int tc64_limb_gemm(const FieldU64& f, uint64_t* C, int64_t ldc, int64_t m, int64_t N, const int32_t* k_ptr,
+                   bool overwrite, const void* EL, const void* BS, int* err, int* status, cudaStream_t s,
+                   bool count_work, int kwork);
+void* tc64_bs_base(void* extra, int64_t m);  // B digit tiles inside the 64-bit update's scratch
 
 template <class F>
 inline size_t trailing_extra_scratch(int64_t m, int64_t n, const RrefPlan& pl) {

@@ -46,6 +46,7 @@ constexpr int32_t MAGIC_I = 0x4B400000;
 struct Params64 {
     uint64_t* C;            // trailing block base: A + j1
     int64_t ldc, m, N;
+    int overwrite;          // 1: C <- E B (C is not read), 0: C <- C + E B
     int m_pad;              // rows per digit plane of E
     int n_tiles;            // 16-column tiles covering N
     const int32_t* panel_k;
@@ -89,11 +90,43 @@ static __global__ void __launch_bounds__(256) split_e64_kernel(const uint64_t* E
     }
 }
 
+// G operand of E = G X for the candidate panel: G[o, t] = -A[o, j0 + cols[t]]
+// for rows that are not pivot rows of this panel, G[prow_t, :] = e_t; eight
+// K-major digit planes of m_pad x 64
+static __global__ void __launch_bounds__(256) split_g64_kernel(const uint64_t* A, int64_t lda, int64_t m, int m_pad,
+                                                               int64_t j0, uint64_t p, const int32_t* panel_k,
+                                                               const int32_t* panel_cols, const int32_t* panel_mark,
+                                                               int gen, __nv_bfloat16* EL) {
+    const int k = *panel_k;
+    if (k == 0) return;
+    const size_t plane = (size_t)m_pad * KMAX;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)m_pad * KMAX;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / KMAX;
+        const int t = (int)(idx - r * KMAX);
+        uint64_t v = 0;
+        if (r < m && t < k) {
+            const int mk = panel_mark[r];
+            if ((mk >> 8) == gen) {
+                v = ((mk & 255) - 1 == t) ? 1ull : 0ull;
+            } else {
+                const uint64_t x = A[r * lda + j0 + panel_cols[t]];
+                v = x ? p - x : 0ull;
+            }
+        }
+        __nv_bfloat16 d[LIMBS];
+        split_digits64(v, p, d);
+#pragma unroll
+        for (int i = 0; i < LIMBS; ++i) EL[i * plane + idx] = d[i];
+    }
+}
+
 // pivot rows of the trailing block (zeroed in C) -> stacked digit tiles of B,
 // one CTA per 16-column tile
+// (rows == nullptr: rows 0 .. k-1; zero_src: zero the gathered rows in C)
 static __global__ void __launch_bounds__(256) gather_split_b64_kernel(uint64_t* C, int64_t ldc, int64_t N,
                                                                       const int32_t* rows, const int32_t* panel_k,
-                                                                      uint64_t p, __nv_bfloat16* BS) {
+                                                                      uint64_t p, __nv_bfloat16* BS, int zero_src) {
     __shared__ uint64_t s[KMAX][BN + 1];
     const int k = *panel_k;
     if (k == 0) return;
@@ -102,9 +135,9 @@ static __global__ void __launch_bounds__(256) gather_split_b64_kernel(uint64_t* 
         const int t = idx / BN, cc = idx % BN;
         uint64_t v = 0;
         if (t < k && c0 + cc < N) {
-            uint64_t* src = C + (int64_t)rows[t] * ldc + c0 + cc;
+            uint64_t* src = C + (int64_t)(rows ? rows[t] : t) * ldc + c0 + cc;
             v = *src;
-            *src = 0ull;
+            if (zero_src) *src = 0ull;
         }
         s[t][cc] = v;
     }
@@ -256,7 +289,7 @@ static __global__ void __launch_bounds__(THREADS, 1)
             const int ncols = (int)((P.N - col0) < 8 ? (P.N - col0) : 8);
             uint64_t old[8];
 #pragma unroll
-            for (int c = 0; c < 8; ++c) old[c] = (row_ok && c < ncols) ? crow[c] : 0ull;
+            for (int c = 0; c < 8; ++c) old[c] = (row_ok && c < ncols && !P.overwrite) ? crow[c] : 0ull;
             const bool got = ptx::mbar_wait(&acc_full[buf], (t >> 1) & 1, &s_err);
             if (!__all_sync(0xffffffffu, got)) {
                 if (lane == 0) flag_error64(P, &s_err);

@@ -26,35 +26,57 @@ bool trailing_tc_u64_available() {
 
 size_t trailing_tc_u64_scratch(int64_t m, int64_t n) { return el64_bytes(m) + bs64_bytes(n) + 1024; }
 
-int trailing_update_tc_u64(const TrailingCtx<FieldU64>& t, cudaStream_t s) {
+// ---- pieces shared by the trailing update and the candidate-panel path
+int tc64_split_e(const uint64_t* E, int64_t ldE, int64_t m, uint64_t p, const int32_t* k_ptr, void* EL,
+                 cudaStream_t s) {
     using namespace tc64;
-    if (t.b > KMAX) { set_error("64-bit tensor-core update needs panels of at most %d columns", KMAX); return LNC_ERR_INVALID; }
-    const uint64_t p = t.f.p;
-    const int m_pad = m_pad64(t.m);
-    const int n_tiles = n_tiles64(t.N);
-    unsigned char* base = (unsigned char*)(((uintptr_t)t.extra + 1023) & ~(uintptr_t)1023);
-    __nv_bfloat16* EL = (__nv_bfloat16*)base;
-    __nv_bfloat16* BS = (__nv_bfloat16*)(base + el64_bytes(t.m));
-    {
-        const int grid = (int)std::min<int64_t>(((int64_t)m_pad * KMAX + 255) / 256, 8192);
-        split_e64_kernel<<<grid, 256, 0, s>>>(t.E, t.ldE, t.m, m_pad, p, t.panel_k, EL);
-        LNC_CHECK_LAUNCH("split_e64_kernel");
-    }
-    gather_split_b64_kernel<<<n_tiles, 256, 0, s>>>(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, p, BS);
+    const int m_pad = m_pad64(m);
+    const int grid = (int)std::min<int64_t>(((int64_t)m_pad * KMAX + 255) / 256, 8192);
+    split_e64_kernel<<<grid, 256, 0, s>>>(E, ldE, m, m_pad, p, k_ptr, (__nv_bfloat16*)EL);
+    LNC_CHECK_LAUNCH("split_e64_kernel");
+    return LNC_OK;
+}
+
+int tc64_split_g(const uint64_t* A, int64_t lda, int64_t m, int64_t j0, uint64_t p, const int32_t* k_ptr,
+                 const int32_t* panel_cols, const int32_t* panel_mark, int gen, void* EL, cudaStream_t s) {
+    using namespace tc64;
+    const int m_pad = m_pad64(m);
+    const int grid = (int)std::min<int64_t>(((int64_t)m_pad * KMAX + 255) / 256, 8192);
+    split_g64_kernel<<<grid, 256, 0, s>>>(A, lda, m, m_pad, j0, p, k_ptr, panel_cols, panel_mark, gen,
+                                          (__nv_bfloat16*)EL);
+    LNC_CHECK_LAUNCH("split_g64_kernel");
+    return LNC_OK;
+}
+
+int tc64_gather_split_b(uint64_t* C, int64_t ldc, int64_t N, const int32_t* rows, const int32_t* k_ptr, uint64_t p,
+                        void* BS, bool zero_src, cudaStream_t s) {
+    tc64::gather_split_b64_kernel<<<n_tiles64(N), 256, 0, s>>>(C, ldc, N, rows, k_ptr, p, (__nv_bfloat16*)BS,
+                                                              zero_src ? 1 : 0);
     LNC_CHECK_LAUNCH("gather_split_b64_kernel");
+    return LNC_OK;
+}
+
+int tc64_limb_gemm(const FieldU64& f, uint64_t* C, int64_t ldc, int64_t m, int64_t N, const int32_t* k_ptr,
+                   bool overwrite, const void* EL, const void* BS, int* err, int* status, cudaStream_t s,
+                   bool count_work, int kwork) {
+    using namespace tc64;
+    const uint64_t p = f.p;
+    const int m_pad = m_pad64(m);
+    const int n_tiles = n_tiles64(N);
     CUtensorMap mapA, mapB;
-    int rc = tc_make_map_bf16(&mapA, EL, KMAX, (uint64_t)LIMBS * m_pad, KC, BM);
-    if (!rc) rc = tc_make_map_bf16(&mapB, BS, KMAX, (uint64_t)n_tiles * B_ROWS, KC, B_ROWS);
+    int rc = tc_make_map_bf16(&mapA, const_cast<void*>(EL), KMAX, (uint64_t)LIMBS * m_pad, KC, BM);
+    if (!rc) rc = tc_make_map_bf16(&mapB, const_cast<void*>(BS), KMAX, (uint64_t)n_tiles * B_ROWS, KC, B_ROWS);
     if (rc) return rc;
     Params64 P{};
-    P.C = t.A + t.j1;
-    P.ldc = t.lda;
-    P.m = t.m;
-    P.N = t.N;
+    P.C = C;
+    P.ldc = ldc;
+    P.m = m;
+    P.N = N;
+    P.overwrite = overwrite ? 1 : 0;
     P.m_pad = m_pad;
     P.n_tiles = n_tiles;
-    P.panel_k = t.panel_k;
-    P.f = t.f;
+    P.panel_k = k_ptr;
+    P.f = f;
     {
         // w_s = 2^(8 s) 2^64 mod p (centred): one Montgomery step of the weighted sum gives sum y_s 2^(8 s)
         unsigned __int128 x = (((unsigned __int128)1) << 64) % p;
@@ -68,15 +90,33 @@ int trailing_update_tc_u64(const TrailingCtx<FieldU64>& t, cudaStream_t s) {
         P.off_lo = (uint64_t)off;
         P.off_hi = (uint64_t)(off >> 64);
     }
-    P.err = t.err;
-    P.status = t.status;
+    P.err = err;
+    P.status = status;
     LNC_CUDA(cudaFuncSetAttribute(limb64_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
     if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }
-    ScopedKernelTimer kt(KC_TRAILING, s, t.predicated ? 0.0 : (double)t.m * (double)t.N * (double)t.b);
+    ScopedKernelTimer kt(KC_TRAILING, s, count_work ? (double)m * (double)N * (double)kwork : 0.0);
     limb64_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(mapA, mapB, P);
     LNC_CHECK_LAUNCH("limb64_gemm_kernel");
     return LNC_OK;
+}
+
+int trailing_update_tc_u64(const TrailingCtx<FieldU64>& t, cudaStream_t s) {
+    using namespace tc64;
+    if (t.b > KMAX) { set_error("64-bit tensor-core update needs panels of at most %d columns", KMAX); return LNC_ERR_INVALID; }
+    unsigned char* base = (unsigned char*)(((uintptr_t)t.extra + 1023) & ~(uintptr_t)1023);
+    void* EL = base;
+    void* BS = base + el64_bytes(t.m);
+    int rc = tc64_split_e(t.E, t.ldE, t.m, t.f.p, t.panel_k, EL, s);
+    if (!rc) rc = tc64_gather_split_b(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, t.f.p, BS, true, s);
+    if (!rc) rc = tc64_limb_gemm(t.f, t.A + t.j1, t.lda, t.m, t.N, t.panel_k, false, EL, BS, t.err, t.status, s,
+                                 !t.predicated, t.b);
+    return rc;
+}
+
+void* tc64_bs_base(void* extra, int64_t m) {
+    unsigned char* base = (unsigned char*)(((uintptr_t)extra + 1023) & ~(uintptr_t)1023);
+    return base + el64_bytes(m);
 }
 
 }  // namespace lnc

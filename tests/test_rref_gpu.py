@@ -236,7 +236,8 @@ def test_panel_paths_agree_on_adversarial_inputs(flags, m, n, r, p):
     assert piv == piv_ref
 
 
-@pytest.mark.parametrize("flags", [0, _lib.LNC_FLAG_SIMT_TRAILING])
+@pytest.mark.parametrize("flags", [0, _lib.LNC_FLAG_SIMT_TRAILING, _lib.LNC_FLAG_ROBUST_PANEL,
+                                   _lib.LNC_FLAG_DEFER_FALLBACK])
 @pytest.mark.parametrize("m,n,p", [(700, 900, 2**61 - 1), (900, 600, 2**32 + 15), (520, 520, 2**64 - 59)])
 def test_u64_tensor_core_update_vs_oracle(flags, m, n, p):
     """64-bit residues: eight-digit limb contraction (default) and the SIMT
@@ -250,6 +251,22 @@ def test_u64_tensor_core_update_vs_oracle(flags, m, n, p):
     A[:40, 100:300] = np.uint64(p - 1)
     A[40:80, 300:500] = np.uint64((p - 1) // 2)
     A[80:90] = np.uint64((p + 1) // 2)
+    out = np.empty_like(A)
+    piv, rank = rref_host_call(A, p, out, flags=flags)
+    R_ref, piv_ref, _ = oracle.rref_modp(A, p)
+    assert np.array_equal(out, R_ref)
+    assert piv == piv_ref
+
+
+@pytest.mark.parametrize("flags", [0, _lib.LNC_FLAG_ROBUST_PANEL])
+def test_u64_candidate_panel_misses_are_redone(flags):
+    """64-bit residues, leading rows zero in the leading columns: the candidate
+    block misses pivots there and the exhaustive panel redoes those panels."""
+    p = 2**61 - 1
+    rng = np.random.default_rng(77)
+    A = rng.integers(0, 2**62, size=(900, 700), dtype=np.uint64) % np.uint64(p)
+    A[:450, :80] = 0
+    A[:, 200:205] = 0
     out = np.empty_like(A)
     piv, rank = rref_host_call(A, p, out, flags=flags)
     R_ref, piv_ref, _ = oracle.rref_modp(A, p)

@@ -52,6 +52,7 @@ WORKLOADS = {
     "rref_u32_8192": dict(m=8192, n=8192, p=P31, dtype="u32"),
     "rref_u32_4096": dict(m=4096, n=4096, p=P31, dtype="u32"),
     "rref_u64_8000": dict(m=8000, n=8000, p=2**61 - 1, dtype="u64"),
+    "rref_u64_4096": dict(m=4096, n=4096, p=2**61 - 1, dtype="u64"),
     # 512 x 640 of rank 384 built as B.C mod 2^31-1 (seed 0), checked against the oracle
     "config1": dict(m=512, n=640, p=P31, dtype="u32", config1=True),
     # uneven batch: m ~ U[64, 2048], n = round(m U[0.8, 1.25]), rank deficit ~ U[0, 10%],
@@ -380,7 +381,7 @@ def run_ours(args, dist: Dist):
                    "parallelism": f"replicas x{dist.world}", "panel_width": 64 if u64 else 128,
                    "trailing": "simt" if args.flags & _lib.LNC_FLAG_SIMT_TRAILING else
                    ("tensor_core (8 digits)" if u64 else "tensor_core (4 digits)"),
-                   "panel": "exhaustive" if (args.flags & (_lib.LNC_FLAG_ROBUST_PANEL | _lib.LNC_FLAG_SIMT_TRAILING)) or u64
+                   "panel": "exhaustive" if args.flags & (_lib.LNC_FLAG_ROBUST_PANEL | _lib.LNC_FLAG_SIMT_TRAILING)
                    else "candidate block + exhaustive fallback",
                    "l2": (f"input {nbytes / 1e6:.0f} MB > L2 (129 MB); no flush needed" if nbytes > 129e6
                           else f"input {nbytes / 1e6:.1f} MB fits L2: inputs restored by a D2D copy each step")},
@@ -442,6 +443,7 @@ def trailing_bytes(m: int, n: int, b: int) -> float:
 PROFILED_TRAFFIC = {
     ("rref_u32_20000", "limb_gemm"): 534.0e6,
     ("rref_u64_8000", "trailing_simt"): 465.4e6,
+    ("rref_u64_8000", "limb_gemm"): 161.1e6,
 }
 
 

@@ -259,13 +259,14 @@ def run_ours(args, dist: Dist):
         _lib.check(L.lnc_rref_device(code, m, n, p, 0.0, d_work.ptr, n, d_out.ptr, n, d_piv.ptr,
                                      d_rank.ptr, stream.handle, args.flags))
 
+    _lib.kernel_timing(True)  # warm-up with the per-kernel events on, so their pool is filled before timing
     for _ in range(args.warmup):
         step()
     stream.synchronize()
     _lib.device_status()
 
     # ---- timed region (device-resident) ----
-    _lib.kernel_timing(True)
+    _lib.kernel_timing(True)  # drains the warm-up's events back into the pool and resets the counters
     ev = [(_lib.Event(), _lib.Event()) for _ in range(args.steps)]
     ev_all = (_lib.Event(), _lib.Event())
     dist.barrier()
@@ -383,6 +384,10 @@ def run_ours(args, dist: Dist):
                    ("tensor_core (8 digits)" if u64 else "tensor_core (4 digits)"),
                    "panel": "exhaustive" if args.flags & (_lib.LNC_FLAG_ROBUST_PANEL | _lib.LNC_FLAG_SIMT_TRAILING)
                    else "candidate block + exhaustive fallback",
+                   "schedule": ("look-ahead: next panel on a second stream during the trailing update"
+                                if not args.flags & (_lib.LNC_FLAG_NO_LOOKAHEAD | _lib.LNC_FLAG_ROBUST_PANEL
+                                                     | _lib.LNC_FLAG_SIMT_TRAILING) and m * n >= 1 << 22
+                                else "one stream"),
                    "l2": (f"input {nbytes / 1e6:.0f} MB > L2 (129 MB); no flush needed" if nbytes > 129e6
                           else f"input {nbytes / 1e6:.1f} MB fits L2: inputs restored by a D2D copy each step")},
         "result_sha256_16": result_hash,
@@ -997,6 +1002,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rref_u32_20000")
     ap.add_argument("--simt", action="store_true", help="force the SIMT trailing update")
     ap.add_argument("--robust-panel", action="store_true", help="force the exhaustive grid-wide panel")
+    ap.add_argument("--no-lookahead", action="store_true", help="F_p: keep every launch on one stream")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--ref-seconds", type=float, default=6.0)
@@ -1017,7 +1023,8 @@ def main():
     else:
         from linac_gb300 import _lib  # fails loudly if the library is missing
         args.flags = (_lib.LNC_FLAG_SIMT_TRAILING if args.simt else 0) | \
-            (_lib.LNC_FLAG_ROBUST_PANEL if args.robust_panel else 0)
+            (_lib.LNC_FLAG_ROBUST_PANEL if args.robust_panel else 0) | \
+            (_lib.LNC_FLAG_NO_LOOKAHEAD if args.no_lookahead else 0)
         if WORKLOADS[args.workload].get("batch"):
             line = run_batch(args, dist)
         elif WORKLOADS[args.workload].get("serve"):

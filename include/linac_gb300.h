@@ -61,6 +61,14 @@ extern "C" {
  * reduced-precision updates could change) the solve is redone in FP64.  Synchronises the
  * stream; lnc_mixed_report describes the last such solve of the thread.     */
 #define LNC_FLAG_MIXED 16
+/* F_p: no look-ahead.  By default a large solve (>= 2^22 entries, at least
+ * three panels) runs the next candidate panel on a second, high-priority
+ * stream while the caller's stream applies the current panel to the columns
+ * beyond it (fork and join through events, so stream capture records both);
+ * this flag keeps every launch on the caller's stream (tests, timing).      */
+#define LNC_FLAG_NO_LOOKAHEAD 32
+/* F_p: look ahead at any shape with at least three panels (tests).         */
+#define LNC_FLAG_LOOKAHEAD 64
 
 /* ---- library / device ---------------------------------------------------- */
 /* Version string of the library. */

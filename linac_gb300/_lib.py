@@ -35,6 +35,8 @@ LNC_FLAG_SIMT_TRAILING = 2
 LNC_FLAG_ROBUST_PANEL = 4
 LNC_FLAG_DEFER_FALLBACK = 8
 LNC_FLAG_MIXED = 16
+LNC_FLAG_NO_LOOKAHEAD = 32
+LNC_FLAG_LOOKAHEAD = 64
 
 KC_PANEL, KC_TRAILING, KC_LOADER, KC_GATHER, KC_BATCH = 0, 1, 2, 3, 4
 

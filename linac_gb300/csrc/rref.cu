@@ -499,6 +499,13 @@ int plan_rref(int64_t m, int64_t n, RrefPlan* plan) {
     if constexpr (F::kDtype == 2) {  // 64-bit residues: the tensor-core update takes 64-column panels
         if (trailing_tc_u64_available()) b = std::min(b, kMaxPanelU64Tc);
     }
+    // look-ahead pays once a trailing update outlasts a candidate panel: matrices of >= 2^22 entries
+    // with at least three panels, on the tensor-core path
+    bool la = false;
+    if constexpr (F::kDtype == 1) la = b == kMaxPanel && trailing_tc_u32_available();
+    if constexpr (F::kDtype == 2) la = b == kPanelU64 && trailing_tc_u64_available();
+    plan->lookahead_ok = la;
+    plan->lookahead = la && m * n >= ((int64_t)1 << 22) && n > 2 * (int64_t)b;
     plan->G = G;
     plan->rows_per_cta = R;
     plan->b = b;
@@ -514,6 +521,58 @@ static size_t fast_extra_scratch(int64_t m, int64_t n) {
            + align_up(sizeof(int32_t) * kMaxPanel, 256)               // panel_cols
            + align_up(sizeof(int32_t) * (size_t)m, 256)               // panel_mark
            + align_up(sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1), 256);  // column -> pivot row
+}
+
+// Look-ahead of the candidate-panel path.  While the caller's stream applies
+// panel q to the columns beyond panel q + 1, a second stream (highest
+// priority, so its one-CTA panel takes the first SM that frees up) runs panel
+// q + 1: candidate block, E = G X and the digit split of E.  That needs its
+// own G digits, a second E digit buffer (panel q's is still being read), its
+// own X digits and a second pivot-count word; the exhaustive fallback of a
+// panel that missed a pivot gets its own transform, pivot rows, count and
+// digit scratch, because its correction of the far columns runs after the
+// fork, next to panel q + 1.
+template <class F>
+static size_t lookahead_scratch(int64_t m, int64_t n, const RrefPlan& pl) {
+    using T = typename F::T;
+    constexpr bool U64 = F::kDtype == 2;
+    constexpr int PW = U64 ? kPanelU64 : kMaxPanel;
+    const size_t el = U64 ? tc64_el_bytes(m) : tc_el_bytes(m);
+    const size_t bsx = U64 ? tc64_bs_bytes(PW) : tc_bs_bytes(PW);
+    return 2 * (el + 1024) + bsx + 1024                      // G digits, second E digits, X digits
+           + align_up(sizeof(T) * (size_t)m * PW, 256)       // fallback transform
+           + align_up(sizeof(int32_t) * PW, 256) + 256       // fallback pivot rows; pivot counts
+           + trailing_extra_scratch<F>(m, n, pl) + 256;      // fallback digit scratch
+}
+
+struct LookaheadStreams {
+    int dev = -1;
+    cudaStream_t main = nullptr;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+static std::mutex g_la_mu;
+static std::vector<LookaheadStreams> g_la;
+
+// The side stream and fork / join events of a caller's stream, created on first
+// use and kept for the process (calls on one stream come from one thread at a time).
+static int lookahead_streams(cudaStream_t main, LookaheadStreams* out) {
+    int dev = 0;
+    LNC_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(g_la_mu);
+    for (const auto& x : g_la)
+        if (x.dev == dev && x.main == main) { *out = x; return LNC_OK; }
+    LookaheadStreams x;
+    x.dev = dev;
+    x.main = main;
+    int lo = 0, hi = 0;
+    LNC_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    LNC_CUDA(cudaStreamCreateWithPriority(&x.side, cudaStreamNonBlocking, hi));
+    LNC_CUDA(cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming));
+    LNC_CUDA(cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming));
+    g_la.push_back(x);
+    *out = x;
+    return LNC_OK;
 }
 
 // Pivots may be found out of column order when a candidate panel is redone by
@@ -573,7 +632,10 @@ size_t rref_scratch_bytes(int64_t m, int64_t n, const RrefPlan& pl) {
     s += align_up(sizeof(T) * (size_t)m * pl.b, 256);           // E
     s += align_up(sizeof(T) * (size_t)pl.b * (size_t)std::max<int64_t>(n, 1), 256);  // Bm
     s += trailing_extra_scratch<F>(m, n, pl);
-    if constexpr (F::kDtype == 1 || F::kDtype == 2) s += fast_extra_scratch(m, n);
+    if constexpr (F::kDtype == 1 || F::kDtype == 2) {
+        s += fast_extra_scratch(m, n);
+        if (pl.lookahead) s += lookahead_scratch<F>(m, n, pl);
+    }
     return s;
 }
 
@@ -774,55 +836,149 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
                 ca.M.r2 = (uint32_t)((((unsigned __int128)1) << 64) % pp);
                 ca.M.mu = f.mu;
             }
-            int gen = 0;
-            for (int64_t j0 = 0; j0 < n; j0 += pl.b) {
-                const int bw = (int)std::min<int64_t>(pl.b, n - j0);
-                const int64_t j1 = j0 + bw;
-                ++gen;
-                ca.j0 = j0;
-                ca.bw = bw;
-                ca.gen = gen;
-                int* miss = defer ? missed_any : missed;
+            // ---- look-ahead buffers (without look-ahead they alias the single-stream ones)
+            const bool la = pl.lookahead && !(flags & LNC_FLAG_NO_LOOKAHEAD);
+            LookaheadStreams ls;
+            void* ELG = EL;            // G digits of E = G X
+            void* ELE[2] = {EL, EL};   // E digits of panels q even / odd
+            void* BSX = BS;            // X digits
+            int32_t* pk[2] = {panel_k, panel_k};
+            T* Efb = E;                // exhaustive fallback: transform, pivot rows, count, digit scratch
+            int32_t* prow_fb = panel_rows;
+            int32_t* pk_fb = panel_k;
+            void* fb_extra = extra;
+            if (la) {
+                int rc0 = lookahead_streams(s, &ls);
+                if (rc0) return rc0;
+                const size_t el = U64 ? tc64_el_bytes(m) : tc_el_bytes(m);
+                const size_t bsx = U64 ? tc64_bs_bytes(PW) : tc_bs_bytes(PW);
+                auto take1k = [&](size_t bytes) {
+                    fx = (unsigned char*)(((uintptr_t)fx + 1023) & ~(uintptr_t)1023);
+                    void* r = fx;
+                    fx += bytes;
+                    return r;
+                };
+                ELG = take1k(el);
+                ELE[1] = take1k(el);
+                BSX = take1k(bsx);
+                fx = (unsigned char*)(((uintptr_t)fx + 255) & ~(uintptr_t)255);
+                Efb = (T*)takef(sizeof(T) * (size_t)m * PW);
+                prow_fb = (int32_t*)takef(sizeof(int32_t) * PW);
+                int32_t* ks = (int32_t*)takef(256);
+                pk[1] = ks;
+                pk_fb = ks + 1;
+                fb_extra = takef(trailing_extra_scratch<F>(m, n, pl));
+                if ((size_t)(fx - (unsigned char*)scratch) > scratch_bytes) {
+                    set_error("internal: scratch layout overflow (look-ahead)");
+                    return LNC_ERR_INVALID;
+                }
+            }
+            TrailingCtx<F> tfb = tctx;  // correction of a redone panel
+            tfb.E = Efb;
+            tfb.panel_k = pk_fb;
+            tfb.panel_rows = prow_fb;
+            tfb.extra = fb_extra;
+            tfb.predicated = true;
+
+            // panel q on stream st: candidate block, G and X digits, E = G X, E digits
+            auto panel_chain = [&](int64_t pj0, int q, cudaStream_t st) -> int {
+                ca.j0 = pj0;
+                ca.bw = (int)std::min<int64_t>(PW, n - pj0);
+                ca.gen = q + 1;
+                ca.panel_k = pk[q & 1];
+                const int32_t* kq = pk[q & 1];
                 int rc = LNC_OK;
                 if constexpr (U64) {
-                    rc = launch_cand_panel64(ca, s);
-                    if (!rc) rc = tc64_split_g(A, lda, m, j0, f.p, panel_k, panel_cols, panel_mark, gen, EL, s);
-                    // E = G X  (m x 64, overwritten)
-                    if (!rc) rc = tc64_gather_split_b(Xbuf, PW, PW, nullptr, panel_k, f.p, BS, false, s);
-                    if (!rc) rc = tc64_limb_gemm(f, E, PW, m, PW, panel_k, true, EL, BS, err, status, s, true, PW);
-                    // A[:, j0:] += E A[P, j0:]  (pivot rows zeroed first)
-                    if (!rc) rc = tc64_split_e(E, PW, m, f.p, panel_k, EL, s);
-                    if (!rc) rc = tc64_gather_split_b(A + j0, lda, n - j0, panel_rows, panel_k, f.p, BS, true, s);
-                    if (!rc) rc = tc64_limb_gemm(f, A + j0, lda, m, n - j0, panel_k, false, EL, BS, err, status, s,
-                                                 true, PW);
-                    if (!rc) rc = launch_check_missed64(A, lda, m, j0, bw, row_used, pivmask, miss, s);
+                    rc = launch_cand_panel64(ca, st);
+                    if (!rc) rc = tc64_split_g(A, lda, m, pj0, f.p, kq, panel_cols, panel_mark, q + 1, ELG, st);
+                    if (!rc) rc = tc64_gather_split_b(Xbuf, PW, PW, nullptr, kq, f.p, BSX, false, st);
+                    if (!rc) rc = tc64_limb_gemm(f, E, PW, m, PW, kq, true, ELG, BSX, err, status, st, true, PW);
+                    if (!rc) rc = tc64_split_e(E, PW, m, f.p, kq, ELE[q & 1], st);
                 } else {
-                    rc = launch_cand_panel(ca, s);
-                    if (!rc) rc = launch_split_g(A, lda, m, j0, f.p, panel_k, panel_cols, panel_mark, gen, EL, s);
-                    // E = G X  (m x 128, overwritten)
-                    if (!rc) rc = tc_gather_split_b(Xbuf, kMaxPanel, kMaxPanel, nullptr, panel_k, f.p, BS, false, s);
-                    if (!rc) rc = tc_limb_gemm(f, E, kMaxPanel, m, kMaxPanel, panel_k, true, EL, BS, n, err, status, s);
-                    // A[:, j0:] += E A[P, j0:]  (pivot rows zeroed first)
-                    if (!rc) rc = tc_split_e(E, kMaxPanel, kMaxPanel, m, f.p, panel_k, EL, s);
-                    if (!rc) rc = tc_gather_split_b(A + j0, lda, n - j0, panel_rows, panel_k, f.p, BS, true, s);
-                    if (!rc) rc = tc_limb_gemm(f, A + j0, lda, m, n - j0, panel_k, false, EL, BS, n, err, status, s);
-                    if (!rc) rc = launch_check_missed(A, lda, m, j0, bw, row_used, pivmask, miss, s);
+                    rc = launch_cand_panel(ca, st);
+                    if (!rc) rc = launch_split_g(A, lda, m, pj0, f.p, kq, panel_cols, panel_mark, q + 1, ELG, st);
+                    if (!rc) rc = tc_gather_split_b(Xbuf, kMaxPanel, kMaxPanel, nullptr, kq, f.p, BSX, false, st);
+                    if (!rc) rc = tc_limb_gemm(f, E, kMaxPanel, m, kMaxPanel, kq, true, ELG, BSX, kMaxPanel, err,
+                                               status, st);
+                    if (!rc) rc = tc_split_e(E, kMaxPanel, kMaxPanel, m, f.p, kq, ELE[q & 1], st);
+                }
+                return rc;
+            };
+            // C[:, c0:c0+N) += E B for the columns of B's digit tiles from column offset off
+            auto apply = [&](int q, int64_t c0, int64_t N, int64_t off, int tpc, cudaStream_t st) -> int {
+                const int32_t* kq = pk[q & 1];
+                if constexpr (U64) {
+                    void* B = (unsigned char*)BS + tc64_bs_bytes(off);
+                    return tc64_limb_gemm(f, A + c0, lda, m, N, kq, false, ELE[q & 1], B, err, status, st, true, PW,
+                                          tpc);
+                } else {
+                    void* B = (unsigned char*)BS + tc_bs_bytes(off);
+                    return tc_limb_gemm(f, A + c0, lda, m, N, kq, false, ELE[q & 1], B, N, err, status, st, true,
+                                        tpc);
+                }
+            };
+
+            int rc = panel_chain(0, 0, s);
+            if (rc) return rc;
+            int q = 0;
+            for (int64_t j0 = 0; j0 < n; j0 += PW, ++q) {
+                const int bw = (int)std::min<int64_t>(PW, n - j0);
+                const int64_t j1 = j0 + bw;
+                // columns updated before the fork: this panel's and the next one's (all of them without look-ahead)
+                const int64_t j2 = la ? std::min<int64_t>(j1 + PW, n) : n;
+                const int32_t* kq = pk[q & 1];
+                int* miss = defer ? missed_any : missed;
+                // A[:, j0:] += E A[P, j0:]  (pivot rows gathered and zeroed first)
+                if constexpr (U64) {
+                    rc = tc64_gather_split_b(A + j0, lda, n - j0, panel_rows, kq, f.p, BS, true, s);
+                } else {
+                    rc = tc_gather_split_b(A + j0, lda, n - j0, panel_rows, kq, f.p, BS, true, s);
+                }
+                if (!rc) rc = apply(q, j0, j2 - j0, 0, la ? 2 : 0, s);
+                if (!rc) {
+                    if constexpr (U64) rc = launch_check_missed64(A, lda, m, j0, bw, row_used, pivmask, miss, s);
+                    else rc = launch_check_missed(A, lda, m, j0, bw, row_used, pivmask, miss, s);
                 }
                 if (rc) return rc;
-                if (defer) continue;
-                // redo the panel exhaustively when the candidate block missed a pivot
-                PanelArgs<F> pa = make_panel_args(j0, bw, j1 < n, missed);
-                rc = launch_panel(pa);
-                if (rc) return rc;
-                if (j1 < n) {
-                    tctx.j1 = j1;
-                    tctx.N = n - j1;
-                    tctx.ldb = n - j1;
-                    tctx.predicated = true;
-                    rc = trailing_update<F>(tctx, s);
-                    tctx.predicated = false;
+                if (!defer) {
+                    // redo the panel exhaustively when the candidate block missed a pivot
+                    PanelArgs<F> pa = make_panel_args(j0, bw, j1 < n, missed);
+                    pa.E = Efb;
+                    pa.panel_k = pk_fb;
+                    pa.panel_rows = prow_fb;
+                    rc = launch_panel(pa);
+                    if (!rc && j1 < n) {
+                        tfb.j1 = j1;
+                        tfb.N = j2 - j1;
+                        tfb.ldb = tfb.N;
+                        rc = trailing_update<F>(tfb, s);
+                    }
                     if (rc) return rc;
                 }
+                if (j1 >= n) break;
+                if (!la) {
+                    rc = panel_chain(j1, q + 1, s);
+                    if (rc) return rc;
+                    continue;
+                }
+                // fork: panel q + 1 on the side stream, columns [j2, n) of panel q here
+                LNC_CUDA(cudaEventRecord(ls.fork, s));
+                LNC_CUDA(cudaStreamWaitEvent(ls.side, ls.fork, 0));
+                rc = panel_chain(j1, q + 1, ls.side);
+                const cudaError_t ej = cudaEventRecord(ls.join, ls.side);
+                if (!rc && j2 < n) {
+                    rc = apply(q, j2, n - j2, j2 - j0, 0, s);
+                    if (!rc && !defer) {
+                        tfb.j1 = j2;
+                        tfb.N = n - j2;
+                        tfb.ldb = tfb.N;
+                        rc = trailing_update<F>(tfb, s);
+                    }
+                }
+                // join (also on failure, so a capture never ends with the side stream's work unjoined)
+                const cudaError_t ew = (ej == cudaSuccess) ? cudaStreamWaitEvent(s, ls.join, 0) : ej;
+                if (rc) return rc;
+                if (ew != cudaSuccess) return cuda_status(ew, "look-ahead join");
             }
             sort_pivots_kernel<<<1, 1024, 0, s>>>(piv_row, piv_col, rank, n, col_row);
             LNC_CHECK_LAUNCH("sort_pivots_kernel");
@@ -925,6 +1081,7 @@ static int rref_device_typed(const F& f, void* work, int64_t ldw, void* out, int
     RrefPlan pl;
     int rc = plan_rref<F>(m, n, &pl);
     if (rc) return rc;
+    if ((flags & LNC_FLAG_LOOKAHEAD) && pl.lookahead_ok && n > 2 * (int64_t)pl.b) pl.lookahead = true;
     size_t sb = rref_scratch_bytes<F>(m, n, pl);
     const bool in_place = (out == work);
     if (in_place) sb += align_up(sizeof(T) * (size_t)m * (size_t)n, 256);
@@ -1194,6 +1351,7 @@ static int rref_noalloc_typed(const F& f, void* work, int64_t ldw, void* out, in
     RrefPlan pl;
     int rc = plan_rref<F>(m, n, &pl);
     if (rc) return rc;
+    pl.lookahead = false;  // one stream: the fixed scratch holds no look-ahead buffers
     const size_t need = rref_scratch_bytes<F>(m, n, pl);
     if (need > kNoAllocScratchBytes) {
         set_error("a %lld x %lld RREF needs %zu bytes of scratch; the fixed no-allocation scratch holds %zu",

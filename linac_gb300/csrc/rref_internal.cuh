@@ -15,6 +15,8 @@ struct RrefPlan {
     int rows_per_cta = 0;  // panel rows held by each CTA
     int b = 0;             // panel width (columns)
     size_t smem = 0;
+    bool lookahead_ok = false;  // the candidate-panel path can look ahead (tensor-core update present)
+    bool lookahead = false;     // ... and does: next panel overlaps the trailing update
 };
 
 template <class F>
@@ -163,7 +165,7 @@ int tc_gather_split_b(uint32_t* C, int64_t ldc, int64_t N, const int32_t* rows, 
                       void* BS, bool zero_src, cudaStream_t s);
 int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t N, const int32_t* k_ptr,
                  bool overwrite, const void* EL, const void* BS, int64_t n_map, int* err, int* status,
-                 cudaStream_t s, bool count_work = true);
+                 cudaStream_t s, bool count_work = true, int tiles_per_cta = 0);
 
 // Candidate-block panel for F_p with 32-bit residues (cand_panel.cu)
 constexpr int kCandThreads = 512;
@@ -224,8 +226,10 @@ int tc64_gather_split_b(uint64_t* C, int64_t ldc, int64_t N, const int32_t* rows
                         void* BS, bool zero_src, cudaStream_t s);
 int tc64_limb_gemm(const FieldU64& f, uint64_t* C, int64_t ldc, int64_t m, int64_t N, const int32_t* k_ptr,
                    bool overwrite, const void* EL, const void* BS, int* err, int* status, cudaStream_t s,
-                   bool count_work, int kwork);
+                   bool count_work, int kwork, int tiles_per_cta = 0);
 void* tc64_bs_base(void* extra, int64_t m);  // B digit tiles inside the 64-bit update's scratch
+size_t tc64_el_bytes(int64_t m);             // E digit planes of m rows
+size_t tc64_bs_bytes(int64_t n);             // B digit tiles of n columns
 
 template <class F>
 inline size_t trailing_extra_scratch(int64_t m, int64_t n, const RrefPlan& pl) {

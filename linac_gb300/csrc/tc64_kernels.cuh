@@ -55,6 +55,7 @@ struct Params64 {
     uint64_t off_lo, off_hi;  // multiple of p >= 2^91 (makes the sum non-negative)
     int* err;
     int* status;
+    int tpc = TILES_PER_CTA;  // 16-column tiles per CTA (grid.x covers n_tiles / tpc)
 };
 
 __device__ __forceinline__ void split_digits64(uint64_t x, uint64_t p, __nv_bfloat16 (&d)[LIMBS]) {
@@ -178,8 +179,8 @@ static __global__ void __launch_bounds__(THREADS, 1)
 
     const int k = *P.panel_k;  // written by an earlier kernel: identical in every thread
     const int rb = blockIdx.y;
-    const int t0 = blockIdx.x * TILES_PER_CTA;
-    const int t1 = min(P.n_tiles, t0 + TILES_PER_CTA);
+    const int t0 = blockIdx.x * P.tpc;
+    const int t1 = min(P.n_tiles, t0 + P.tpc);
     if (k == 0 || t1 <= t0) return;
     const int ntiles = t1 - t0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

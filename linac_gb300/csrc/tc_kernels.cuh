@@ -80,6 +80,7 @@ struct TcParams {
     double* Cd;             // float epilogue (see LimbJob)
     const double* rscale;
     const double* cscale;
+    int tpc = TILES_PER_CTA;  // 32-column tiles per CTA (grid.x covers n_tiles / tpc)
 };
 
 __device__ __forceinline__ void split_digits(uint32_t x, uint32_t p, uint32_t half, __nv_bfloat16 (&d)[LIMBS]) {
@@ -521,8 +522,8 @@ static __global__ void __launch_bounds__(THREADS, 1)
     J.m = P.m;
     J.N = P.N;
     J.rb = blockIdx.y;
-    J.t0 = blockIdx.x * TILES_PER_CTA;
-    J.t1 = min(P.n_tiles, J.t0 + TILES_PER_CTA);
+    J.t0 = blockIdx.x * P.tpc;
+    J.t1 = min(P.n_tiles, J.t0 + P.tpc);
     J.a_row0 = 0;
     J.a_plane = P.m_pad;
     J.b_row0 = 0;

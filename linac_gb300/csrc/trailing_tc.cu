@@ -151,7 +151,7 @@ int tc_gather_split_b(uint32_t* C, int64_t ldc, int64_t N, const int32_t* rows, 
 
 int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t N, const int32_t* k_ptr,
                  bool overwrite, const void* EL, const void* BS, int64_t n_map, int* err, int* status,
-                 cudaStream_t s, bool count_work) {
+                 cudaStream_t s, bool count_work, int tiles_per_cta) {
     using namespace tc;
     const int m_pad = m_pad_of(m);
     const int n_tiles = n_tiles_of(N);
@@ -186,9 +186,10 @@ int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t
     P.err = err;
     P.status = status;
     P.redc = redc ? 1 : 0;
+    P.tpc = tiles_per_cta > 0 ? tiles_per_cta : TILES_PER_CTA;
     auto kern = redc ? limb_gemm_kernel<EPI_REDC> : limb_gemm_kernel<EPI_BARRETT>;
     LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
-    dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
+    dim3 grid((unsigned)((n_tiles + P.tpc - 1) / P.tpc), (unsigned)(m_pad / BM));
     if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }
     ScopedKernelTimer kt(KC_TRAILING, s, count_work ? (double)m * (double)N * (double)KMAX : 0.0);
     kern<<<grid, THREADS, SMEM_BYTES, s>>>(mapA, mapB, P);
@@ -205,8 +206,9 @@ int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s) {
     if (rc) return rc;
     rc = tc_gather_split_b(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, p, BS, true, s);
     if (rc) return rc;
+    // a predicated update (a fallback that usually finds nothing) launches few, wide CTAs: they exit at once
     return tc_limb_gemm(t.f, t.A + t.j1, t.lda, t.m, t.N, t.panel_k, false, EL, BS, t.n, t.err, t.status, s,
-                        !t.predicated);
+                        !t.predicated, t.predicated ? 64 : 0);
 }
 
 // C = A B mod p (32-bit residues, any sizes): the limb GEMM applied to

@@ -58,7 +58,7 @@ int tc64_gather_split_b(uint64_t* C, int64_t ldc, int64_t N, const int32_t* rows
 
 int tc64_limb_gemm(const FieldU64& f, uint64_t* C, int64_t ldc, int64_t m, int64_t N, const int32_t* k_ptr,
                    bool overwrite, const void* EL, const void* BS, int* err, int* status, cudaStream_t s,
-                   bool count_work, int kwork) {
+                   bool count_work, int kwork, int tiles_per_cta) {
     using namespace tc64;
     const uint64_t p = f.p;
     const int m_pad = m_pad64(m);
@@ -92,8 +92,9 @@ int tc64_limb_gemm(const FieldU64& f, uint64_t* C, int64_t ldc, int64_t m, int64
     }
     P.err = err;
     P.status = status;
+    P.tpc = tiles_per_cta > 0 ? tiles_per_cta : TILES_PER_CTA;
     LNC_CUDA(cudaFuncSetAttribute(limb64_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
-    dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
+    dim3 grid((unsigned)((n_tiles + P.tpc - 1) / P.tpc), (unsigned)(m_pad / BM));
     if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }
     ScopedKernelTimer kt(KC_TRAILING, s, count_work ? (double)m * (double)N * (double)kwork : 0.0);
     limb64_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(mapA, mapB, P);
@@ -109,10 +110,14 @@ int trailing_update_tc_u64(const TrailingCtx<FieldU64>& t, cudaStream_t s) {
     void* BS = base + el64_bytes(t.m);
     int rc = tc64_split_e(t.E, t.ldE, t.m, t.f.p, t.panel_k, EL, s);
     if (!rc) rc = tc64_gather_split_b(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, t.f.p, BS, true, s);
+    // a predicated update (a fallback that usually finds nothing) launches few, wide CTAs: they exit at once
     if (!rc) rc = tc64_limb_gemm(t.f, t.A + t.j1, t.lda, t.m, t.N, t.panel_k, false, EL, BS, t.err, t.status, s,
-                                 !t.predicated, t.b);
+                                 !t.predicated, t.b, t.predicated ? 64 : 0);
     return rc;
 }
+
+size_t tc64_el_bytes(int64_t m) { return el64_bytes(m); }
+size_t tc64_bs_bytes(int64_t n) { return bs64_bytes(n); }
 
 void* tc64_bs_base(void* extra, int64_t m) {
     unsigned char* base = (unsigned char*)(((uintptr_t)extra + 1023) & ~(uintptr_t)1023);

@@ -49,8 +49,17 @@ struct ArithSmall {  // odd p < 2^31: 32-bit Montgomery, reductions by unsigned 
     }
     __device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b) const { return red((uint64_t)a * b); }
     __device__ __forceinline__ uint32_t prep(uint32_t v) const { return v; }
-    // Shoup's constant of a fixed multiplier v: floor(v 2^32 / p)
-    __device__ __forceinline__ uint32_t aux(uint32_t v) const { return (uint32_t)(((uint64_t)v << 32) / M.p); }
+    // Shoup's constant of a fixed multiplier v < p: floor(v 2^32 / p), by Barrett division with
+    // mu = floor((2^64 - 1) / p): the estimate falls short by at most two (integer pipe only;
+    // this part's FP64 rate is far too low for a per-column quotient)
+    __device__ __forceinline__ uint32_t aux(uint32_t v) const {
+        const uint64_t x = (uint64_t)v << 32;
+        uint64_t q = __umul64hi(x, M.mu);
+        uint64_t r = x - q * (uint64_t)M.p;
+        if (r >= M.p) { ++q; r -= M.p; }
+        if (r >= M.p) ++q;
+        return (uint32_t)q;
+    }
     // x - f v mod p with v's Shoup constant vs: q = floor(f vs / 2^32) undershoots f v / p by at
     // most 1, so f v - q p lies in [0, 2p) (computed mod 2^32; 2p < 2^32)
     __device__ __forceinline__ uint32_t mulsub(uint32_t x, uint32_t f, uint32_t v, uint32_t vs) const {
@@ -66,6 +75,19 @@ struct ArithSmall {  // odd p < 2^31: 32-bit Montgomery, reductions by unsigned 
         return min(d, d + M.p);
     }
     __device__ __forceinline__ uint32_t inverse(uint32_t a) const { return inv_binary<uint32_t>(a, M.p); }
+    // fraction-free step  a x - f v  with both fixed factors prepared (value, Shoup constant)
+    using Pre = uint2;
+    __device__ __forceinline__ uint32_t neg(uint32_t f) const { return f ? M.p - f : 0u; }
+    __device__ __forceinline__ Pre pre_ff(uint32_t v) const { return make_uint2(v, aux(v)); }
+    __device__ __forceinline__ uint32_t shoup(uint32_t x, uint2 w) const {  // x w mod p, any 32-bit x
+        const uint32_t q = __umulhi(x, w.y);
+        const uint32_t r = x * w.x - q * M.p;
+        return min(r, r - M.p);
+    }
+    __device__ __forceinline__ uint32_t ffsub(uint32_t x, uint2 a, uint32_t f, uint2 v) const {
+        const uint32_t d = shoup(x, a) - shoup(f, v);
+        return min(d, d + M.p);
+    }
 };
 struct ArithMont {  // odd p >= 2^31
     Mont32 M;
@@ -78,6 +100,12 @@ struct ArithMont {  // odd p >= 2^31
     __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return M.montmul(M.to_mont(a), b); }
     __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
     __device__ __forceinline__ uint32_t inverse(uint32_t a) const { return inv_binary<uint32_t>(a, M.p); }
+    using Pre = uint32_t;  // Montgomery form
+    __device__ __forceinline__ uint32_t neg(uint32_t f) const { return f ? M.p - f : 0u; }
+    __device__ __forceinline__ Pre pre_ff(uint32_t v) const { return M.to_mont(v); }
+    __device__ __forceinline__ uint32_t ffsub(uint32_t x, Pre a, uint32_t f, Pre v) const {
+        return M.sub(M.montmul(x, a), M.montmul(f, v));
+    }
 };
 struct ArithTwo {  // p = 2
     Mont32 M;
@@ -90,6 +118,12 @@ struct ArithTwo {  // p = 2
     __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return M.barrett((uint64_t)a * b); }
     __device__ __forceinline__ uint32_t sub(uint32_t a, uint32_t b) const { return M.sub(a, b); }
     __device__ __forceinline__ uint32_t inverse(uint32_t) const { return 1u; }
+    using Pre = uint32_t;
+    __device__ __forceinline__ uint32_t neg(uint32_t f) const { return f; }  // -1 = 1 mod 2
+    __device__ __forceinline__ Pre pre_ff(uint32_t v) const { return v; }
+    __device__ __forceinline__ uint32_t ffsub(uint32_t x, Pre a, uint32_t f, Pre v) const {
+        return (x & a) ^ (f & v);  // residues 0 / 1
+    }
 };
 
 struct Arith64 {  // 64-bit residues (odd p < 2^64): Montgomery with R = 2^64
@@ -102,6 +136,12 @@ struct Arith64 {  // 64-bit residues (odd p < 2^64): Montgomery with R = 2^64
     }
     __device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) const { return F.mul(a, b); }
     __device__ __forceinline__ uint64_t inverse(uint64_t a) const { return inv_binary<uint64_t>(a, F.p); }
+    using Pre = uint64_t;  // Montgomery form
+    __device__ __forceinline__ uint64_t neg(uint64_t f) const { return f ? F.p - f : 0ull; }
+    __device__ __forceinline__ Pre pre_ff(uint64_t v) const { return F.to_mont(v); }
+    __device__ __forceinline__ uint64_t ffsub(uint64_t x, Pre a, uint64_t f, Pre v) const {
+        return F.sub(F.montmul(x, a), F.montmul(f, v));
+    }
 };
 
 // arithmetic policies are built from the panel arguments

@@ -26,9 +26,47 @@
 
 #include <cuda_bf16.h>
 
-#include "cand_kernels.cuh"
+#include "cand_cluster.cuh"
 
 namespace lnc {
+
+template <class Arith, class W, int PW, int CL>
+static __global__ void __launch_bounds__(kCandClusterThreads, 1)
+    cand_cluster_kernel(const __grid_constant__ CandArgs a) {
+    cand_cluster_body<Arith, W, PW, CL>(a);
+}
+
+// CTAs of the cluster panel: 8 by default; LNC_CAND_CLUSTER=4 selects four, =0 the one-CTA panel.
+static int cluster_panel_ctas() {
+    static int ctas = -1;
+    if (ctas < 0) {
+        const char* env = getenv("LNC_CAND_CLUSTER");
+        ctas = (env && env[0] == '0') ? 0 : (env && env[0] == '4') ? 4 : 8;
+    }
+    return ctas;
+}
+
+template <class Arith, class W, int PW, int CL>
+static int launch_cand_cluster(const CandArgs& a, double elt, cudaStream_t s) {
+    auto kern = cand_cluster_kernel<Arith, W, PW, CL>;
+    const size_t smem = cand_cluster_smem<W, PW, CL>(a.smax);
+    ScopedKernelTimer kt(KC_PANEL, s, 2.0 * a.smax * a.bw * elt);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CL, 1, 1);
+    cfg.blockDim = dim3(kCandClusterThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    LNC_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+    LNC_CHECK_LAUNCH("cand_cluster_kernel");
+    return LNC_OK;
+}
 
 template <class Arith>
 static int launch_cand_typed(const CandArgs& a, size_t smem, cudaStream_t s) {
@@ -40,6 +78,17 @@ static int launch_cand_typed(const CandArgs& a, size_t smem, cudaStream_t s) {
 }
 
 int launch_cand_panel(const CandArgs& a, cudaStream_t s) {
+    const int cl = cluster_panel_ctas();
+    if (cl == 8) {
+        if (!(a.M.p & 1u)) return launch_cand_cluster<ArithTwo, uint32_t, kMaxPanel, 8>(a, 4.0, s);
+        if (a.M.p < (1u << 31)) return launch_cand_cluster<ArithSmall, uint32_t, kMaxPanel, 8>(a, 4.0, s);
+        return launch_cand_cluster<ArithMont, uint32_t, kMaxPanel, 8>(a, 4.0, s);
+    }
+    if (cl == 4) {
+        if (!(a.M.p & 1u)) return launch_cand_cluster<ArithTwo, uint32_t, kMaxPanel, 4>(a, 4.0, s);
+        if (a.M.p < (1u << 31)) return launch_cand_cluster<ArithSmall, uint32_t, kMaxPanel, 4>(a, 4.0, s);
+        return launch_cand_cluster<ArithMont, uint32_t, kMaxPanel, 4>(a, 4.0, s);
+    }
     const size_t smem = (size_t)(a.smax | 1) * kMaxPanel * 4 + 2 * kMaxPanel * 4 + 256 * 4;
     if (!(a.M.p & 1u)) return launch_cand_typed<ArithTwo>(a, smem, s);
     if (a.M.p < (1u << 31)) return launch_cand_typed<ArithSmall>(a, smem, s);
@@ -47,6 +96,9 @@ int launch_cand_panel(const CandArgs& a, cudaStream_t s) {
 }
 
 int launch_cand_panel64(const CandArgs& a, cudaStream_t s) {
+    const int cl = cluster_panel_ctas();
+    if (cl == 8) return launch_cand_cluster<Arith64, uint64_t, kPanelU64, 8>(a, 8.0, s);
+    if (cl == 4) return launch_cand_cluster<Arith64, uint64_t, kPanelU64, 4>(a, 8.0, s);
     const size_t smem = cand_smem<uint64_t, kPanelU64>(a.smax);
     auto kern = cand_panel_kernel<Arith64, uint64_t, kPanelU64>;
     LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

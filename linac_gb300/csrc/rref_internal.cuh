@@ -160,7 +160,7 @@ size_t tc_el_bytes(int64_t m);
 size_t tc_bs_bytes(int64_t n);
 int tc_m_pad(int64_t m);
 int tc_split_e(const uint32_t* E, int64_t ldE, int b, int64_t m, uint32_t p, const int32_t* k_ptr, void* EL,
-               cudaStream_t s);
+               cudaStream_t s, int max_grid = 0);
 int tc_gather_split_b(uint32_t* C, int64_t ldc, int64_t N, const int32_t* rows, const int32_t* k_ptr, uint32_t p,
                       void* BS, bool zero_src, cudaStream_t s);
 int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t N, const int32_t* k_ptr,
@@ -219,7 +219,7 @@ size_t trailing_tc_u64_scratch(int64_t m, int64_t n);
 bool trailing_tc_u64_available();
 constexpr int kMaxPanelU64Tc = 64;
 int tc64_split_e(const uint64_t* E, int64_t ldE, int64_t m, uint64_t p, const int32_t* k_ptr, void* EL,
-                 cudaStream_t s);
+                 cudaStream_t s, int max_grid = 0);
 int tc64_split_g(const uint64_t* A, int64_t lda, int64_t m, int64_t j0, uint64_t p, const int32_t* k_ptr,
                  const int32_t* panel_cols, const int32_t* panel_mark, int gen, void* EL, cudaStream_t s);
 int tc64_gather_split_b(uint64_t* C, int64_t ldc, int64_t N, const int32_t* rows, const int32_t* k_ptr, uint64_t p,

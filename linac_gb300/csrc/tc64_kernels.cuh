@@ -132,17 +132,28 @@ static __global__ void __launch_bounds__(256) gather_split_b64_kernel(uint64_t* 
     const int k = *panel_k;
     if (k == 0) return;
     const int64_t c0 = (int64_t)blockIdx.x * BN;
-    for (int idx = threadIdx.x; idx < KMAX * BN; idx += blockDim.x) {
+    constexpr int PER = KMAX * BN / 256;  // entries per thread (blockDim.x == 256)
+    uint64_t v[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {  // every load issued before any is used
+        const int idx = threadIdx.x + 256 * j;
         const int t = idx / BN, cc = idx % BN;
-        uint64_t v = 0;
-        if (t < k && c0 + cc < N) {
-            uint64_t* src = C + (int64_t)(rows ? rows[t] : t) * ldc + c0 + cc;
-            v = *src;
-            if (zero_src) *src = 0ull;
-        }
-        s[t][cc] = v;
+        v[j] = (t < k && c0 + cc < N) ? C[(int64_t)(rows ? rows[t] : t) * ldc + c0 + cc] : 0ull;
+    }
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+        const int idx = threadIdx.x + 256 * j;
+        s[idx / BN][idx % BN] = v[j];
     }
     __syncthreads();
+    if (zero_src) {  // after the loads have returned
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const int idx = threadIdx.x + 256 * j;
+            const int t = idx / BN, cc = idx % BN;
+            if (t < k && c0 + cc < N) C[(int64_t)(rows ? rows[t] : t) * ldc + c0 + cc] = 0ull;
+        }
+    }
     __nv_bfloat16* dst = BS + (size_t)blockIdx.x * B_ROWS * KMAX;
     for (int idx = threadIdx.x; idx < BN * KMAX; idx += blockDim.x) {
         const int cc = idx / KMAX, t = idx % KMAX;

@@ -145,16 +145,20 @@ __device__ __forceinline__ void gather_split_b_body(int tile, uint32_t* C, int64
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
         const int row = s_rows[w + 8 * r];
-        v[r] = 0u;
-        if (row >= 0 && col_ok) {
-            uint32_t* a = base + (int64_t)row * ldc;
-            v[r] = *a;
-            if (zero_src) *a = 0u;  // does not wait for the load's data
-        }
+        v[r] = (row >= 0 && col_ok) ? base[(int64_t)row * ldc] : 0u;
     }
 #pragma unroll
     for (int r = 0; r < RPW; ++r) s[w + 8 * r][lane] = v[r];
     __syncthreads();
+    // the rows are zeroed only after every load has returned (a store right behind a load of the
+    // same address holds the thread until that load completes, serialising the 16 round trips)
+    if (zero_src) {
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+            const int row = s_rows[w + 8 * r];
+            if (row >= 0 && col_ok) base[(int64_t)row * ldc] = 0u;
+        }
+    }
     // row (i, cc) of this tile's stacked block holds digit i of column cc for t = 0..127
     // (two consecutive t per thread: 4-byte stores, 128 contiguous bytes per warp)
     __nv_bfloat16* dst = BS + (size_t)tile * B_ROWS * KMAX;

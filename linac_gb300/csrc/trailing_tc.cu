@@ -130,11 +130,11 @@ size_t tc_bs_bytes(int64_t n) {
 int tc_m_pad(int64_t m) { return tc::m_pad_of(m); }
 
 int tc_split_e(const uint32_t* E, int64_t ldE, int b, int64_t m, uint32_t p, const int32_t* k_ptr, void* EL,
-               cudaStream_t s) {
+               cudaStream_t s, int max_grid) {
     using namespace tc;
     const int m_pad = m_pad_of(m);
     const int64_t total = (int64_t)m_pad * KMAX;
-    const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
+    const int grid = (int)std::min<int64_t>((total + 255) / 256, max_grid > 0 ? max_grid : 4096);
     split_e_kernel<<<grid, 256, 0, s>>>(E, ldE, b, m, m_pad, p, k_ptr, (__nv_bfloat16*)EL);
     LNC_CHECK_LAUNCH("split_e_kernel");
     return LNC_OK;
@@ -202,13 +202,14 @@ int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s) {
     void* EL = base;
     void* BS = base + tc_el_bytes(t.m);
     const uint32_t p = t.f.p;
-    int rc = tc_split_e(t.E, t.ldE, t.b, t.m, p, t.panel_k, EL, s);
+    // a predicated update (a fallback that usually finds nothing) launches few CTAs, one per row
+    // block for the contraction: they read the pivot count and exit
+    int rc = tc_split_e(t.E, t.ldE, t.b, t.m, p, t.panel_k, EL, s, t.predicated ? 152 : 0);
     if (rc) return rc;
     rc = tc_gather_split_b(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, p, BS, true, s);
     if (rc) return rc;
-    // a predicated update (a fallback that usually finds nothing) launches few, wide CTAs: they exit at once
     return tc_limb_gemm(t.f, t.A + t.j1, t.lda, t.m, t.N, t.panel_k, false, EL, BS, t.n, t.err, t.status, s,
-                        !t.predicated, t.predicated ? 64 : 0);
+                        !t.predicated, t.predicated ? (1 << 20) : 0);
 }
 
 // C = A B mod p (32-bit residues, any sizes): the limb GEMM applied to

@@ -28,10 +28,10 @@ size_t trailing_tc_u64_scratch(int64_t m, int64_t n) { return el64_bytes(m) + bs
 
 // ---- pieces shared by the trailing update and the candidate-panel path
 int tc64_split_e(const uint64_t* E, int64_t ldE, int64_t m, uint64_t p, const int32_t* k_ptr, void* EL,
-                 cudaStream_t s) {
+                 cudaStream_t s, int max_grid) {
     using namespace tc64;
     const int m_pad = m_pad64(m);
-    const int grid = (int)std::min<int64_t>(((int64_t)m_pad * KMAX + 255) / 256, 8192);
+    const int grid = (int)std::min<int64_t>(((int64_t)m_pad * KMAX + 255) / 256, max_grid > 0 ? max_grid : 8192);
     split_e64_kernel<<<grid, 256, 0, s>>>(E, ldE, m, m_pad, p, k_ptr, (__nv_bfloat16*)EL);
     LNC_CHECK_LAUNCH("split_e64_kernel");
     return LNC_OK;
@@ -108,11 +108,12 @@ int trailing_update_tc_u64(const TrailingCtx<FieldU64>& t, cudaStream_t s) {
     unsigned char* base = (unsigned char*)(((uintptr_t)t.extra + 1023) & ~(uintptr_t)1023);
     void* EL = base;
     void* BS = base + el64_bytes(t.m);
-    int rc = tc64_split_e(t.E, t.ldE, t.m, t.f.p, t.panel_k, EL, s);
+    // a predicated update (a fallback that usually finds nothing) launches few CTAs, one per row
+    // block for the contraction: they read the pivot count and exit
+    int rc = tc64_split_e(t.E, t.ldE, t.m, t.f.p, t.panel_k, EL, s, t.predicated ? 152 : 0);
     if (!rc) rc = tc64_gather_split_b(t.A + t.j1, t.lda, t.N, t.panel_rows, t.panel_k, t.f.p, BS, true, s);
-    // a predicated update (a fallback that usually finds nothing) launches few, wide CTAs: they exit at once
     if (!rc) rc = tc64_limb_gemm(t.f, t.A + t.j1, t.lda, t.m, t.N, t.panel_k, false, EL, BS, t.err, t.status, s,
-                                 !t.predicated, t.b, t.predicated ? 64 : 0);
+                                 !t.predicated, t.b, t.predicated ? (1 << 20) : 0);
     return rc;
 }
 

@@ -967,7 +967,9 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
                 rc = panel_chain(j1, q + 1, ls.side);
                 const cudaError_t ej = cudaEventRecord(ls.join, ls.side);
                 if (!rc && j2 < n) {
-                    rc = apply(q, j2, n - j2, j2 - j0, 0, s);
+                    // 16 tiles per CTA, not the wave-fitted count: many short CTAs free SMs for the
+                    // side stream's cluster more often than a grid of exactly filled waves
+                    rc = apply(q, j2, n - j2, j2 - j0, 16, s);
                     if (!rc && !defer) {
                         tfb.j1 = j2;
                         tfb.N = n - j2;

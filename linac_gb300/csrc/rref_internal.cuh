@@ -155,6 +155,12 @@ int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s);
 size_t trailing_tc_u32_scratch(int64_t m, int64_t n, int b);
 bool trailing_tc_u32_available();
 
+// Tiles per CTA of a limb contraction over row_blocks x n_tiles tiles: the
+// grid's waves (CTAs over the SM count) times the tiles each CTA runs plus
+// its fixed start-up (E digits load, TMEM allocation; about 0.6 tile),
+// minimised over 4 .. 48 (trailing_tc.cu).
+int limb_tiles_per_cta(int n_tiles, int row_blocks);
+
 // Reusable tensor-core pieces (trailing_tc.cu)
 size_t tc_el_bytes(int64_t m);
 size_t tc_bs_bytes(int64_t n);

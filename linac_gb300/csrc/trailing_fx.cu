@@ -222,10 +222,11 @@ int trailing_update_fx(const TrailingCtx<F>& t, cudaStream_t s) {
     P.Cd = (double*)(t.A + t.j1);
     P.rscale = rscale;
     P.cscale = cscale;
+    P.tpc = limb_tiles_per_cta(n_tiles, m_pad / BM);
     constexpr int EPI = CPLX ? EPI_C128 : EPI_F64;
     auto kern = limb_gemm_kernel<EPI>;
     LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
-    dim3 grid((unsigned)((n_tiles + TILES_PER_CTA - 1) / TILES_PER_CTA), (unsigned)(m_pad / BM));
+    dim3 grid((unsigned)((n_tiles + P.tpc - 1) / P.tpc), (unsigned)(m_pad / BM));
     if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }
     ScopedKernelTimer kt(KC_TRAILING, s, (double)t.m * (double)t.N * (double)t.b * (CPLX ? 4.0 : 1.0));
     kern<<<grid, THREADS, SMEM_BYTES, s>>>(mapA, mapB, P);

@@ -129,6 +129,23 @@ size_t tc_bs_bytes(int64_t n) {
 }
 int tc_m_pad(int64_t m) { return tc::m_pad_of(m); }
 
+int limb_tiles_per_cta(int n_tiles, int row_blocks) {
+    DeviceInfo di;
+    const int sms = (device_info(&di) == LNC_OK && di.sms > 0) ? di.sms : 148;
+    int best = 16;
+    double best_cost = 1e300;
+    for (int t = 4; t <= 48; ++t) {
+        const long long ctas = (long long)row_blocks * ((n_tiles + t - 1) / t);
+        const long long waves = (ctas + sms - 1) / sms;
+        const double c = (double)waves * ((double)std::min(t, n_tiles) + 0.6);
+        if (c < best_cost - 1e-9) {
+            best_cost = c;
+            best = t;
+        }
+    }
+    return best;
+}
+
 int tc_split_e(const uint32_t* E, int64_t ldE, int b, int64_t m, uint32_t p, const int32_t* k_ptr, void* EL,
                cudaStream_t s, int max_grid) {
     using namespace tc;
@@ -186,7 +203,7 @@ int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t
     P.err = err;
     P.status = status;
     P.redc = redc ? 1 : 0;
-    P.tpc = tiles_per_cta > 0 ? tiles_per_cta : TILES_PER_CTA;
+    P.tpc = tiles_per_cta > 0 ? tiles_per_cta : limb_tiles_per_cta(n_tiles, m_pad / BM);
     auto kern = redc ? limb_gemm_kernel<EPI_REDC> : limb_gemm_kernel<EPI_BARRETT>;
     LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     dim3 grid((unsigned)((n_tiles + P.tpc - 1) / P.tpc), (unsigned)(m_pad / BM));

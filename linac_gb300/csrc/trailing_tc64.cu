@@ -92,7 +92,7 @@ int tc64_limb_gemm(const FieldU64& f, uint64_t* C, int64_t ldc, int64_t m, int64
     }
     P.err = err;
     P.status = status;
-    P.tpc = tiles_per_cta > 0 ? tiles_per_cta : TILES_PER_CTA;
+    P.tpc = tiles_per_cta > 0 ? tiles_per_cta : limb_tiles_per_cta(n_tiles, m_pad / BM);
     LNC_CUDA(cudaFuncSetAttribute(limb64_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     dim3 grid((unsigned)((n_tiles + P.tpc - 1) / P.tpc), (unsigned)(m_pad / BM));
     if (grid.y > 65535) { set_error("trailing update: too many row blocks"); return LNC_ERR_UNSUPPORTED; }

@@ -59,6 +59,18 @@ def test_u64_random_and_missed(m, n, p):
     _check(A, p, LA)
 
 
+@pytest.mark.parametrize("m,n,p", [(40, 2000, 2**31 - 1), (3000, 300, 4294967291), (161, 700, 2**61 - 1),
+                                   (7, 1300, 2)])
+def test_extreme_aspect_ratios(m, n, p):
+    """Short-wide (fewer rows than a candidate block: the block holds every
+    remaining row) and tall-skinny inputs, and a ragged last panel."""
+    rng = np.random.default_rng(m + n)
+    dt = np.uint64 if p > 2**32 else np.uint32
+    A = (rng.integers(0, 2**62, size=(m, n), dtype=np.uint64) % np.uint64(p)).astype(dt)
+    A[:, 130:140] = 0
+    _check(A, p, LA)
+
+
 def test_deferred_fallback_reports_a_miss_with_lookahead():
     p = 2**31 - 1
     rng = np.random.default_rng(5)

@@ -448,7 +448,7 @@ def trailing_bytes(m: int, n: int, b: int) -> float:
 PROFILED_TRAFFIC = {
     ("rref_u32_20000", "limb_gemm"): 322.0e6,   # look-ahead schedule: near, far and E = G X launches
     ("rref_u64_8000", "trailing_simt"): 465.4e6,
-    ("rref_u64_8000", "limb_gemm"): 161.1e6,    # one-stream schedule
+    ("rref_u64_8000", "limb_gemm"): 97.4e6,     # look-ahead schedule
 }
 
 

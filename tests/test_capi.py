@@ -39,6 +39,17 @@ def test_python_binding_covers_header():
                                            "lnc_rref_device_noalloc", "lnc_rref_refine")), n
 
 
+def test_header_constants_match_the_python_binding():
+    """Every status, dtype and flag #define of the header has the same value in
+    linac_gb300._lib (the ctypes layer passes them through unchanged)."""
+    text = open(os.path.join(ROOT, "include", "linac_gb300.h")).read()
+    defines = dict(re.findall(r"#define\s+(LNC_(?:OK|ERR_[A-Z_]+|U32|U64|F64|C128|FLAG_[A-Z_]+))\s+\(?(-?\d+)\)?",
+                              text))
+    assert len(defines) >= 20
+    for name, value in defines.items():
+        assert getattr(_lib, name) == int(value), name
+
+
 def test_version_and_device_count():
     assert b"sm_103a" in _lib.lib().lnc_version()
     assert _lib.device_count() >= 0

@@ -1321,7 +1321,7 @@ int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol
 // address is obtained once per device with cudaGetSymbolAddress, on that
 // device's first call of lnc_rref_device_noalloc (so make that first call
 // before any stream capture).  All calls share the array and it keeps the
-// previous call's contents; the driver clears everything that must start at
+// previous call's contents; rref_run clears everything that must start at
 // zero.  Calls that overlap on the GPU (concurrent streams, or devices not
 // yet synchronised between calls) race on the array.
 // ----------------------------------------------------------------------------

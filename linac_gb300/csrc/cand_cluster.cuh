@@ -8,28 +8,32 @@
 // what the step needs: the pivot row index, the pivot value and the pivot
 // column's entries (the multipliers), pushed by the owner of that column into
 // every CTA's shared memory (distributed shared memory, double-buffered by
-// step parity) ahead of one cluster barrier.
+// step parity) and released at a cluster barrier.
 //
 // The elimination is fraction-free, so no inverse sits on the per-column
 // chain: step s with pivot row p, pivot value a and multipliers f updates
 // every other row as  x <- a x - f_i v  (v: the pivot row's entry in that
 // column) and leaves row p as it is.  The pivot column itself becomes the
 // transform column (-f_i, and 1 in row p), and earlier transform columns are
-// updated like any other column, so after the last step the pivot columns
-// hold T[:, P] for the product T of the step matrices.  With a_s the pivot
-// value of step s, S_u = a_0 ... a_(u-1) and the row of pivot t scaled by
-// d_t = a_t a_(t+1) ... a_(k-1), the pivot block's inverse is
-//     X[t][u] = T[p_t, p_u] S_u / d_t = T[p_t, p_u] S_u S_t / (a_0 ... a_(k-1)),
-// so one inverse per panel (of the product of all pivots) replaces one per
+// updated like any other column.  For the product T of the step matrices,
+// the column of pivot u then holds T[:, p_u] / S_u with S_u = a_0 ... a_(u-1)
+// (row p_u was scaled by every earlier step before it became a pivot row),
+// and T A[P, Q] is diagonal with entries d_t = a_t a_(t+1) ... a_(k-1), so the
+// pivot block's inverse is
+//     X[t][u] = col_u[p_t] S_u / d_t = col_u[p_t] S_u S_t / (a_0 ... a_(k-1)):
+// one inverse per panel (of the product of all pivots) replaces one per
 // column.  Pivot choice (first candidate row, in candidate order, with a
 // non-zero entry) and therefore every output equal the single-CTA panel's:
 // fraction-free values are non-zero multiples of the normalised ones.
 //
 // Look-ahead: while the other warps apply step s, warp 0 of the CTA owning
-// column s + 1 updates that column first, picks its pivot row and pushes
-// step s + 1's data, so the cluster barrier at the end of step s is the only
-// wait.  All CTAs run the same number of cluster barriers (one before the
-// loop, one per column, one at the end); no CTA returns early.
+// column s + 1 updates that column first, picks its pivot row, pushes step
+// s + 1's data and arrives at the cluster barrier with release semantics; the
+// other threads arrive (relaxed) as soon as they have read step s's slot, and
+// every thread waits at the start of the next step.  All threads alternate
+// arrive and wait the same number of times (one full barrier before the
+// loop, one phase per column, one full barrier at the end); no CTA returns
+// early.
 #pragma once
 
 #include "cand_kernels.cuh"

@@ -1,7 +1,11 @@
 // Seeded synthetic residues on the device (benchmark and test inputs): entry
 // i of a fill is a SplitMix64 hash of (seed, i) mapped to [0, p) by a
 // 64 x 64 -> high-64 multiply (bias below 2^-32 for p < 2^32).
+//
+// Also the 64-bit-residue product C = A B mod p used to certify solves of
+// augmented systems [A | B] (A X = B mod p) and to build inputs on the device.
 #include "common.cuh"
+#include "field.cuh"
 
 namespace lnc {
 
@@ -35,6 +39,46 @@ int fill_uniform_dispatch(void* dev, int64_t count, uint64_t p, uint64_t seed, i
         return LNC_ERR_INVALID;
     }
     LNC_CHECK_LAUNCH("fill_uniform_kernel");
+    return LNC_OK;
+}
+
+// C = A B mod p for 64-bit residues (odd p): 16 x 16 output tiles, 16-deep
+// slices of A and B staged in shared memory, B converted to Montgomery form
+// on load so that one Montgomery product per term gives a b mod p.  A SIMT
+// kernel: its use (certificates, narrow right-hand sides) is small next to
+// the elimination.
+constexpr int kMatTile = 16;
+__global__ void __launch_bounds__(kMatTile * kMatTile) matmul_u64_kernel(FieldU64 f, const uint64_t* A, int64_t lda,
+                                                                         const uint64_t* B, int64_t ldb, uint64_t* C,
+                                                                         int64_t ldc, int64_t m, int64_t k, int64_t n) {
+    __shared__ uint64_t As[kMatTile][kMatTile + 1];
+    __shared__ uint64_t Bs[kMatTile][kMatTile + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int64_t row = (int64_t)blockIdx.y * kMatTile + ty;
+    const int64_t col = (int64_t)blockIdx.x * kMatTile + tx;
+    uint64_t acc = 0;
+    for (int64_t t0 = 0; t0 < k; t0 += kMatTile) {
+        const int64_t ta = t0 + tx, tb = t0 + ty;
+        As[ty][tx] = (row < m && ta < k) ? f.reduce_input(A[row * lda + ta]) : 0ull;
+        Bs[ty][tx] = (tb < k && col < n) ? f.to_mont(f.reduce_input(B[tb * ldb + col])) : 0ull;
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < kMatTile; ++u) acc = f.add(acc, f.montmul(As[ty][u], Bs[u][tx]));
+        __syncthreads();
+    }
+    if (row < m && col < n) C[row * ldc + col] = acc;
+}
+
+int matmul_modp_u64(uint64_t p, int64_t m, int64_t k, int64_t n, const uint64_t* A, int64_t lda, const uint64_t* B,
+                    int64_t ldb, uint64_t* C, int64_t ldc, cudaStream_t s) {
+    if (m <= 0 || n <= 0) return LNC_OK;
+    if ((p & 1) == 0 || p < 3) { set_error("matmul: 64-bit residues need an odd p > 2"); return LNC_ERR_INVALID; }
+    const int64_t gy = (m + kMatTile - 1) / kMatTile, gx = (n + kMatTile - 1) / kMatTile;
+    if (gy > 65535) { set_error("matmul: at most %d rows", 65535 * kMatTile); return LNC_ERR_UNSUPPORTED; }
+    if (gx > INT32_MAX) { set_error("matmul: too many columns"); return LNC_ERR_UNSUPPORTED; }
+    matmul_u64_kernel<<<dim3((unsigned)gx, (unsigned)gy), dim3(kMatTile, kMatTile), 0, s>>>(
+        FieldU64::make(p), A, lda, B, ldb, C, ldc, m, k, n);
+    LNC_CHECK_LAUNCH("matmul_u64_kernel");
     return LNC_OK;
 }
 

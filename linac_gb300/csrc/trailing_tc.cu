@@ -231,6 +231,9 @@ int trailing_update_tc_u32(const TrailingCtx<FieldU32>& t, cudaStream_t s) {
 
 // C = A B mod p (32-bit residues, any sizes): the limb GEMM applied to
 // 128-deep slices of the contraction, the first slice overwriting C.
+int matmul_modp_u64(uint64_t p, int64_t m, int64_t k, int64_t n, const uint64_t* A, int64_t lda, const uint64_t* B,
+                    int64_t ldb, uint64_t* C, int64_t ldc, cudaStream_t s);
+
 int tc_matmul_modp(uint32_t p, int64_t m, int64_t k, int64_t n, const uint32_t* A, int64_t lda,
                    const uint32_t* B, int64_t ldb, uint32_t* C, int64_t ldc, cudaStream_t s) {
     using namespace tc;
@@ -277,9 +280,18 @@ int tc_matmul_modp(uint32_t p, int64_t m, int64_t k, int64_t n, const uint32_t* 
 extern "C" int lnc_matmul_modp_device(int dtype, int64_t m, int64_t k, int64_t n, uint64_t p, const void* A,
                                       int64_t lda, const void* B, int64_t ldb, void* C, int64_t ldc, void* stream) {
     using namespace lnc;
-    if (dtype != LNC_U32) { set_error("matmul: LNC_U32 only"); return LNC_ERR_UNSUPPORTED; }
-    if (p < 2 || p > 0xFFFFFFFFull) { set_error("matmul: 2 <= p < 2^32"); return LNC_ERR_INVALID; }
+    if (m < 0 || k < 0 || n < 0) { set_error("matmul: negative shape"); return LNC_ERR_INVALID; }
     if (lda < k || ldb < n || ldc < n) { set_error("matmul: leading dimension too small"); return LNC_ERR_INVALID; }
+    if (dtype == LNC_U64) {
+        if (k == 0) {
+            if (m > 0 && n > 0) LNC_CUDA(cudaMemset2DAsync(C, 8 * ldc, 0, 8 * n, m, (cudaStream_t)stream));
+            return LNC_OK;
+        }
+        return matmul_modp_u64(p, m, k, n, (const uint64_t*)A, lda, (const uint64_t*)B, ldb, (uint64_t*)C, ldc,
+                               (cudaStream_t)stream);
+    }
+    if (dtype != LNC_U32) { set_error("matmul: LNC_U32 or LNC_U64"); return LNC_ERR_UNSUPPORTED; }
+    if (p < 2 || p > 0xFFFFFFFFull) { set_error("matmul: 2 <= p < 2^32"); return LNC_ERR_INVALID; }
     return tc_matmul_modp((uint32_t)p, m, k, n, (const uint32_t*)A, lda, (const uint32_t*)B, ldb, (uint32_t*)C, ldc,
                           (cudaStream_t)stream);
 }

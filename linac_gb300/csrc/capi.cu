@@ -195,6 +195,18 @@ int validate_rref_args(int dtype, int64_t m, int64_t n, uint64_t p, int64_t ld) 
     return LNC_OK;
 }
 
+int check_loader_indices(const uint32_t* lind, int64_t n_cols, int64_t degree, int64_t basis_len) {
+    const int64_t count = n_cols * degree;
+    for (int64_t i = 0; i < count; ++i) {
+        if ((int64_t)lind[i] >= basis_len) {
+            set_error("loader: lindices[%lld, %lld] = %u refers past the end of a bases row (length %lld)",
+                      (long long)(i / degree), (long long)(i % degree), lind[i], (long long)basis_len);
+            return LNC_ERR_INVALID;
+        }
+    }
+    return LNC_OK;
+}
+
 int load_matrix_dispatch(int dtype, int64_t n_rows, int64_t n_cols, int64_t basis_len, int64_t degree,
                          uint64_t p, const void* bases, const uint32_t* lind, void* out, int64_t ldo,
                          cudaStream_t s);
@@ -314,11 +326,21 @@ int lnc_mixed_report(int* iterations, double* last_correction, int* redone_fp64)
     return mixed_report(iterations, last_correction, redone_fp64);
 }
 
+int lnc_mixed_error_estimate(double* error_estimate) {
+    if (!error_estimate) { set_error("null argument"); return LNC_ERR_INVALID; }
+    *error_estimate = mixed_error_estimate();
+    return LNC_OK;
+}
+
 int lnc_device_status(void) {
     LNC_CUDA(cudaDeviceSynchronize());
     int st = 0;
     int rc = rref_read_and_clear_status(&st);
     if (rc) return rc;
+    if (st == LNC_ERR_INVALID) {
+        set_error("a loader index referred past the end of a bases row (those columns were written as 0)");
+        return st;
+    }
     if (st != 0) {
         set_error("a bounded device-side wait timed out (status %d)", st);
         return st;
@@ -446,8 +468,11 @@ int lnc_load_matrix_host(int dtype, int64_t n_rows, int64_t n_cols, int64_t basi
     if (elt == 0) { set_error("unknown dtype %d", dtype); return LNC_ERR_INVALID; }
     if (n_rows < 0 || n_cols < 0 || basis_len < 0 || degree < 0) { set_error("loader: bad shape"); return LNC_ERR_INVALID; }
     if (n_rows == 0 || n_cols == 0) return LNC_OK;
+    if (degree < 1 || basis_len < 1) { set_error("loader: degree and basis length must be >= 1"); return LNC_ERR_INVALID; }
+    int rc = check_loader_indices(hlind, n_cols, degree, basis_len);
+    if (rc) return rc;
     cudaStream_t s;
-    int rc = library_stream(&s);
+    rc = library_stream(&s);
     if (rc) return rc;
     const size_t bb = elt * (size_t)n_rows * (size_t)basis_len;
     const size_t lb = sizeof(uint32_t) * (size_t)n_cols * (size_t)degree;

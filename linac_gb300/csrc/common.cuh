@@ -67,6 +67,9 @@ int device_info(DeviceInfo* out);
 size_t dtype_size(int dtype);
 bool is_prime_u64(uint64_t n);
 int validate_rref_args(int dtype, int64_t m, int64_t n, uint64_t p, int64_t ld);
+// LNC_ERR_INVALID (with a message) when a host index list refers past the
+// end of a bases row.
+int check_loader_indices(const uint32_t* host_lindices, int64_t n_cols, int64_t degree, int64_t basis_len);
 
 constexpr int kMaxPanel = 128;           // widest panel (columns)
 constexpr int kPanelThreads = 256;

@@ -398,6 +398,8 @@ int lnc_serve_submit(void* server, const lnc_serve_request* req, int64_t* ticket
     Server* S = (Server*)server;
     if (!S || !req || !ticket) { set_error("serve: null argument"); return LNC_ERR_INVALID; }
     int rc = validate_request(*req);
+    if (!rc && req->kind == LNC_SERVE_LOAD_RREF)  // the host index list must be readable at submission
+        rc = check_loader_indices(req->host_lindices, req->n, req->degree, req->basis_len);
     if (rc) return rc;
     const int prev = [&] { int d = 0; cudaGetDevice(&d); return d; }();
     if (prev != S->device) cudaSetDevice(S->device);

@@ -207,4 +207,16 @@ def load_matrices(prefactors, ansatze, points, use_cuda=True, _use_galois=True, 
                                        _real=real, verbose=verbose))
         else:
             As.append(np.empty((bases.shape[0], 0), dtype="uint32"))
+    if _single_point(points, ansatze):
+        # one point given as scalars: the reference's bases are 1-D and it returns the
+        # matrices' only rows (linac/pycuda_matrix_loader.py:191,228-229)
+        return [A[0] for A in As]
     return As
+
+
+def _single_point(points, ansatze) -> bool:
+    """True for dict-form points whose variables hold scalars (one point)."""
+    if not isinstance(points, dict):
+        return False
+    names = {"1"} | set(_flatten(ansatze))
+    return all(np.ndim(points[v]) == 0 for v in names if v in points)

@@ -80,6 +80,18 @@ def test_bad_arguments_rejected():
     assert rc == _lib.LNC_ERR_INVALID
 
 
+def test_loader_host_entry_rejects_out_of_range_index():
+    """Checked on the host before any device work (no GPU needed)."""
+    L = _lib.lib()
+    bases = np.ones((4, 3), dtype=np.uint32)
+    lind = np.array([[0, 1], [2, 3]], dtype=np.uint32)  # 3 is one past a row of 3
+    out = np.zeros((4, 2), dtype=np.uint32)
+    rc = L.lnc_load_matrix_host(_lib.LNC_U32, 4, 2, 3, 2, 2**31 - 1, bases.ctypes.data, lind.ctypes.data,
+                                out.ctypes.data)
+    assert rc == _lib.LNC_ERR_INVALID
+    assert "lindices[1, 1]" in _lib.last_error()
+
+
 def test_empty_shapes_need_no_device():
     for shape in ((0, 5), (5, 0), (0, 0)):
         out = cuda_row_reduce(np.zeros(shape, dtype=np.uint32), 2**31 - 1)

@@ -10,8 +10,9 @@
  *
  * The reference (GDeLaurentis/linac v1.0.1) exposes Python functions backed by
  * pycuda, not a C ABI; each entry point below names the reference interface it
- * replaces.  INTEGRATION.md shows the ctypes binding that the reference-side
- * Python would use.
+ * replaces.  The library keeps per-device state (streams, cached device
+ * properties, the no-allocation scratch address) for the life of the process;
+ * none of it survives cudaDeviceReset.
  */
 #ifndef LINAC_GB300_H
 #define LINAC_GB300_H
@@ -103,8 +104,10 @@ int lnc_event_create(void** event);
 int lnc_event_destroy(void* event);
 int lnc_event_record(void* event, void* stream);
 int lnc_event_elapsed_ms(void* start, void* stop, float* ms);
-/* Read (and clear) the device-side error word that bounded waits set; returns
- * the status it held (LNC_OK when none).  Synchronises the device. */
+/* Read (and clear) the device-side error word; returns the status it held
+ * (LNC_OK when none): LNC_ERR_TIMEOUT from a bounded wait that ran out,
+ * LNC_ERR_INVALID from lnc_load_matrix_device given an index past the end of
+ * a bases row.  Synchronises the device. */
 int lnc_device_status(void);
 
 /* ---- kernel timing (CUDA events on the launching stream) ------------------ */
@@ -154,11 +157,12 @@ int lnc_rref_device(int dtype, int64_t m, int64_t n, uint64_t p, double tol, voi
  * when they need the result -- a host framework that reserved all of HBM for
  * its own pool up front, or a latency-critical thread that must not wait on an
  * allocator.  No counterpart in the reference (linac always allocates through
- * pycuda).  Limits: dev_out must differ from dev_work; sizes whose scratch
- * exceeds 16 MiB (about m + n > 30,000 for uint32 residues) are rejected with
- * LNC_ERR_INVALID.  The first call on a device looks up the array's device
- * address (make it before any stream capture); all calls share the array, so
- * calls that overlap on the GPU race.
+ * pycuda).  Limits: dev_out must not overlap dev_work at all; sizes whose
+ * scratch exceeds 16 MiB (about m + n > 30,000 for uint32 residues) are
+ * rejected with LNC_ERR_INVALID.  The first call on a device looks up the
+ * array's device address (make it before any stream capture) and keeps it
+ * for the life of the process (it does not survive cudaDeviceReset); all
+ * calls share the array, so calls that overlap on the GPU race.
  */
 int lnc_rref_device_noalloc(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* dev_work,
                             int64_t ld_work, void* dev_out, int64_t ld_out, int64_t* dev_pivot_cols,
@@ -199,11 +203,34 @@ int lnc_batch_plan_destroy(void* plan);
 /* create + run + finish + destroy */
 int lnc_rref_batch_device(int dtype, const lnc_batch_matrix* mats, int64_t count, void* stream, int flags);
 
+/* ---- batched float / complex RREF --------------------------------------------- */
+typedef struct lnc_mixed_result {
+    int iterations;        /* refinement iterations (LNC_FLAG_MIXED)                   */
+    int redone_fp64;       /* 1: a rank decision was close, the solve was redone in FP64 */
+    double error_estimate; /* as lnc_mixed_error_estimate; 0 without LNC_FLAG_MIXED     */
+} lnc_mixed_result;
+
+/*
+ * RREF of `count` float64 / complex128 matrices of any sizes (LNC_F64 or
+ * LNC_C128; `p` of each descriptor is ignored), `tol` the head threshold
+ * (<= 0: 1e-9), flags as for lnc_rref_device (LNC_FLAG_MIXED for the
+ * mixed-precision path).  `workers` host threads (<= 0: 8), each with its own
+ * stream, take the matrices in order and solve them concurrently; inputs are
+ * not modified.  reports (optional, count entries) receives each solve's
+ * mixed-precision report.  Synchronous.
+ * No counterpart in the reference: linac reduces one matrix per
+ * cuda_row_reduce call (linac/pycuda_row_reduce.py:18-151).
+ */
+int lnc_rref_float_batch(int dtype, const lnc_batch_matrix* mats, int64_t count, double tol, int flags,
+                         int workers, lnc_mixed_result* reports);
+
 /* ---- workload helpers (no counterpart in the reference) --------------------- */
 /* Fill `count` residues uniform in [0, p) from `seed` (LNC_U32 / LNC_U64). */
 int lnc_fill_uniform_modp(void* dev_ptr, int64_t count, uint64_t p, uint64_t seed, int dtype, void* stream);
-/* C = A B mod p, A m x k, B k x n, exact (LNC_U32, tensor-core limb GEMM);
- * used to build rank-deficient inputs B.C on the device. */
+/* C = A B mod p, A m x k, B k x n, exact: LNC_U32 (p < 2^32) on the
+ * tensor-core limb GEMM, LNC_U64 (odd p) on a SIMT Montgomery kernel.  Used
+ * to build rank-deficient inputs B.C on the device and to certify the RREF
+ * [I | X] of an augmented system [A | B] (A X = B mod p). */
 int lnc_matmul_modp_device(int dtype, int64_t m, int64_t k, int64_t n, uint64_t p, const void* A, int64_t lda,
                            const void* B, int64_t ldb, void* C, int64_t ldc, void* stream);
 
@@ -212,6 +239,14 @@ int lnc_matmul_modp_device(int dtype, int64_t m, int64_t k, int64_t n, uint64_t 
  * entries, and whether the solve was redone in FP64.  No reference
  * counterpart (linac's float path is FP64 only, linac/row_reduce.cu:55-270). */
 int lnc_mixed_report(int* iterations, double* last_correction, int* redone_fp64);
+/* Error estimate of the calling thread's last LNC_FLAG_MIXED solve: the
+ * max-norm of one further refinement correction (FP64 residual of the result
+ * through the stored panel transforms, computed and not applied) relative to
+ * the largest refined entry -- an a-posteriori estimate of the result's
+ * max-norm error against the exact RREF of the row-scaled input.  0 when no
+ * entry needed refinement (full column rank: the result is exact), -1 when
+ * the solve was redone in FP64.  No reference counterpart. */
+int lnc_mixed_error_estimate(double* error_estimate);
 
 /* ---- incremental RREF --------------------------------------------------------- */
 /*
@@ -251,7 +286,11 @@ int lnc_canonical_kernel_device(int dtype, int64_t r, int64_t n, uint64_t p, con
  * out[r, c] = prod_{t<degree} bases[r, lindices[c, t]] (mod p for LNC_U32 /
  * LNC_U64; plain products for LNC_F64 / LNC_C128), folded left to right; a
  * single factor is copied as is.  bases is n_rows x basis_len, lindices is
- * n_cols x degree (uint32), out is n_rows x n_cols (ld_out).
+ * n_cols x degree (uint32), out is n_rows x n_cols (ld_out).  An index >=
+ * basis_len is an error: the host entry returns LNC_ERR_INVALID before any
+ * device work; the device entry (which cannot read the indices on the host)
+ * writes 0 to the affected columns and raises the device error word to
+ * LNC_ERR_INVALID (lnc_device_status).
  * Replaces cuda_load_matrix (linac/pycuda_matrix_loader.py:27-124) and its
  * kernel LoadMatrix (linac/matrix_loader.cu:88-112).
  */

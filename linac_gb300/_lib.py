@@ -101,6 +101,7 @@ _SIGNATURES = {
     "lnc_load_matrix_device": ([_int, _i64, _i64, _i64, _i64, _u64, _vp, _vp, _vp, _i64, _vp], _int),
     "lnc_fill_uniform_modp": ([_vp, _i64, _u64, _u64, _int, _vp], _int),
     "lnc_mixed_report": ([_vp, _vp, _vp], _int),
+    "lnc_mixed_error_estimate": ([_vp], _int),
     "lnc_canonical_kernel_device": ([_int, _i64, _i64, _u64, _vp, _i64, _vp, _vp, _i64, _vp], _int),
     "lnc_rref_append_device": ([_int, _i64, _i64, _i64, _u64, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp],
                                _int),
@@ -324,4 +325,7 @@ def mixed_report() -> dict:
     """Outcome of this thread's last mixed-precision float solve."""
     it, corr, redone = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_int(0)
     check(lib().lnc_mixed_report(ctypes.byref(it), ctypes.byref(corr), ctypes.byref(redone)), "lnc_mixed_report")
-    return {"iterations": it.value, "last_correction": corr.value, "redone_fp64": bool(redone.value)}
+    est = ctypes.c_double(0)
+    check(lib().lnc_mixed_error_estimate(ctypes.byref(est)), "lnc_mixed_error_estimate")
+    return {"iterations": it.value, "last_correction": corr.value, "redone_fp64": bool(redone.value),
+            "error_estimate": None if est.value < 0 else est.value}

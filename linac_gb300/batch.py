@@ -46,7 +46,12 @@ def _bind():
     _lib.bind("lnc_batch_plan_bytes", [vp], i64)
     _lib.bind("lnc_batch_plan_destroy", [vp])
     _lib.bind("lnc_rref_batch_device", [ci, vp, i64, vp, ci])
+    _lib.bind("lnc_rref_float_batch", [ci, vp, i64, ctypes.c_double, ci, ci, vp])
     _bound = True
+
+
+class lnc_mixed_result(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("redone_fp64", ctypes.c_int), ("error_estimate", ctypes.c_double)]
 
 
 def _align(x: int, a: int = 256) -> int:
@@ -179,6 +184,107 @@ def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True)
         return res
     finally:
         plan.close()
+
+
+class FloatBatch:
+    """Device buffers for a list of float64 / complex128 matrices (inputs and
+    outputs packed, 256-byte aligned) and the descriptors of
+    lnc_rref_float_batch; ``run`` solves them all."""
+
+    def __init__(self, shapes, dtype):
+        _bind()
+        self.dtype = np.dtype(dtype)
+        if self.dtype not in (np.dtype(np.float64), np.dtype(np.complex128)):
+            raise ValueError("float batches hold float64 or complex128 matrices")
+        self.code = _lib.DTYPE_CODE[self.dtype]
+        self.shapes = [(int(m), int(n)) for m, n in shapes]
+        elt = self.dtype.itemsize
+        self.offsets, off = [], 0
+        for m, n in self.shapes:
+            self.offsets.append(off)
+            off += _align(elt * m * n)
+        self.total_bytes = off
+        self.d_in = _lib.DeviceBuffer(off)
+        self.d_out = _lib.DeviceBuffer(off)
+        kmax = [min(m, n) for m, n in self.shapes]
+        self.piv_off = np.concatenate([[0], np.cumsum(kmax)]).astype(np.int64)
+        self.d_piv = _lib.DeviceBuffer(8 * int(self.piv_off[-1]) + 8)
+        self.d_rank = _lib.DeviceBuffer(8 * max(1, len(self.shapes)))
+        descs = (lnc_batch_matrix * max(1, len(self.shapes)))()
+        for i, (m, n) in enumerate(self.shapes):
+            d = descs[i]
+            d.p, d.m, d.n = 0, m, n
+            d.dev_in = self.d_in.ptr + self.offsets[i]
+            d.ld_in = n
+            d.dev_out = self.d_out.ptr + self.offsets[i]
+            d.ld_out = n
+            d.dev_pivot_cols = self.d_piv.ptr + 8 * int(self.piv_off[i])
+            d.dev_rank = self.d_rank.ptr + 8 * i
+        self._descs = descs
+        self.reports = (lnc_mixed_result * max(1, len(self.shapes)))()
+
+    def pack(self, matrices) -> np.ndarray:
+        buf = _lib.PinnedArray((self.total_bytes,), np.uint8).array
+        for (m, n), off, A in zip(self.shapes, self.offsets, matrices):
+            np.copyto(buf[off:off + self.dtype.itemsize * m * n].view(self.dtype).reshape(m, n), A)
+        return buf
+
+    def upload(self, packed: np.ndarray, stream=None):
+        _lib.check(_lib.lib().lnc_memcpy_h2d(self.d_in.ptr, packed.ctypes.data, self.total_bytes, stream))
+        _lib.check(_lib.lib().lnc_stream_synchronize(stream))
+
+    def run(self, mixed: bool = True, workers: int = 8, tol: float = 1e-9):
+        flags = _lib.LNC_FLAG_MIXED if mixed else 0
+        _lib.check(_lib.lib().lnc_rref_float_batch(self.code, ctypes.addressof(self._descs), len(self.shapes),
+                                                   float(tol), flags, int(workers),
+                                                   ctypes.addressof(self.reports)), "lnc_rref_float_batch")
+
+    def download(self, packed: np.ndarray | None = None, stream=None) -> np.ndarray:
+        packed = packed if packed is not None else _lib.PinnedArray((self.total_bytes,), np.uint8).array
+        _lib.check(_lib.lib().lnc_memcpy_d2h(packed.ctypes.data, self.d_out.ptr, self.total_bytes, stream))
+        _lib.check(_lib.lib().lnc_stream_synchronize(stream))
+        return packed
+
+    def unpack(self, packed: np.ndarray):
+        return [packed[off:off + self.dtype.itemsize * m * n].view(self.dtype).reshape(m, n)
+                for (m, n), off in zip(self.shapes, self.offsets)]
+
+    def pivots_and_ranks(self):
+        piv = np.empty(int(self.piv_off[-1]) + 1, dtype=np.int64)
+        self.d_piv.download(piv)
+        ranks = np.empty(max(1, len(self.shapes)), dtype=np.int64)
+        self.d_rank.download(ranks)
+        return [list(piv[self.piv_off[i]:self.piv_off[i] + ranks[i]]) for i in range(len(self.shapes))], \
+            ranks[:len(self.shapes)]
+
+    def report_list(self):
+        return [{"iterations": r.iterations, "redone_fp64": bool(r.redone_fp64),
+                 "error_estimate": None if r.redone_fp64 else r.error_estimate}
+                for r in self.reports[:len(self.shapes)]]
+
+
+def rref_float_batch(matrices, mixed: bool = True, workers: int = 8, return_pivots: bool = False,
+                     return_reports: bool = False, tol: float = 1e-9):
+    """RREF of every float64 / complex128 matrix of the list (linac's float
+    semantics: rows pre-scaled by their largest |a|, partial pivoting,
+    threshold ``tol``), solved concurrently by ``workers`` host threads on
+    their own streams.  ``mixed=True`` uses the mixed-precision path (its
+    per-matrix reports, with the error estimate, when ``return_reports``).
+    All matrices take one element type: complex128 if any is complex."""
+    mats = [np.asarray(A) for A in matrices]
+    cplx = any(np.iscomplexobj(A) and np.any(A.imag) for A in mats)
+    dt = np.complex128 if cplx else np.float64
+    fb = FloatBatch([A.shape for A in mats], dt)
+    fb.upload(fb.pack([A.real if (not cplx and np.iscomplexobj(A)) else A for A in mats]))
+    fb.run(mixed=mixed, workers=workers, tol=tol)
+    res = [R.copy() for R in fb.unpack(fb.download())]
+    out = [res]
+    if return_pivots:
+        pivs, _ = fb.pivots_and_ranks()
+        out.append([[int(x) for x in p] for p in pivs])
+    if return_reports:
+        out.append(fb.report_list())
+    return out[0] if len(out) == 1 else tuple(out)
 
 
 # ---------------------------------------------------------------------------

@@ -1121,6 +1121,7 @@ struct MixedReport {
     int iterations = 0;
     double last_correction = 0.0;
     int redone = 0;
+    double error_estimate = 0.0;  // -1 when the solve was redone in FP64 (not estimated)
 };
 static thread_local MixedReport t_mixed;
 
@@ -1187,6 +1188,7 @@ static int rref_mixed_typed(const F& f, void* work, int64_t ldw, void* out, int6
     if (unc) {
         // a rank decision within reach of the reduced precision: redo in FP64 from the scaled input
         t_mixed.redone = 1;
+        t_mixed.error_estimate = -1.0;
         LNC_CUDA(cudaMemcpy2DAsync(work, sizeof(T) * ldw, mx.As, sizeof(T) * n, sizeof(T) * n, m,
                                    cudaMemcpyDeviceToDevice, s));
         rc = rref_run<F>(f, (T*)work, m, n, ldw, R, n, nullptr, nullptr, s, run_flags | LNC_FLAG_NO_SCALING, blk,
@@ -1223,35 +1225,49 @@ static int rref_mixed_typed(const F& f, void* work, int64_t ldw, void* out, int6
         unsigned long long* stats = (unsigned long long*)(rb + z_b + r_b + g_b + i_b);
         LNC_CUDA(cudaMemcpyAsync(d_colmap, colmap.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
         LNC_CUDA(cudaMemcpyAsync(d_nc, nc.data(), sizeof(int32_t) * qn, cudaMemcpyHostToDevice, s));
-        double prev = INFINITY;
-        for (int it = 0; it < 10 && !rc; ++it) {
-            rc = refine_build_z<T>(n, qn, d_colmap, d_nc, R, n, Z, s);
-            if (!rc) {
-                LNC_CUDA(cudaMemsetAsync(Res, 0, sizeof(T) * (size_t)m * qn, s));
-                rc = refine_narrow_gemm<T>(m, qn, n, nullptr, mx.As, n, Z, qn, Res, qn, s);
+        // one correction: Res = A_s Z (the FP64 residual of the current result), Res <- M Res
+        // through the stored panel transforms, then R += Res on the refined entries (or, with
+        // apply = false, only the max-norms of the correction and of the entries are measured)
+        auto correction = [&](bool apply, double* corr, double* ymax) -> int {
+            int r2 = refine_build_z<T>(n, qn, d_colmap, d_nc, R, n, Z, s);
+            if (!r2) {
+                cudaError_t e2 = cudaMemsetAsync(Res, 0, sizeof(T) * (size_t)m * qn, s);
+                if (e2 != cudaSuccess) return cuda_status(e2, "cudaMemsetAsync");
+                r2 = refine_narrow_gemm<T>(m, qn, n, nullptr, mx.As, n, Z, qn, Res, qn, s);
             }
-            for (int64_t pq = 0; pq < panels && !rc; ++pq) {  // Res <- M Res, panel by panel
+            for (int64_t pq = 0; pq < panels && !r2; ++pq) {  // Res <- M Res, panel by panel
                 dim3 g((unsigned)std::max<int64_t>(1, std::min<int64_t>((qn + 255) / 256, 64)), (unsigned)pl.b);
                 gather_pivot_rows_kernel<F><<<g, 256, 0, s>>>(f, Res, qn, 0, qn, mx.P_all + pq * pl.b,
                                                               mx.K_all + pq, Bg, qn);
                 LNC_CHECK_LAUNCH("gather_pivot_rows_kernel (refinement)");
-                rc = refine_narrow_gemm<T>(m, qn, pl.b, mx.K_all + pq, mx.E_all + pq * pl.b, mx.ldE, Bg, qn, Res, qn,
+                r2 = refine_narrow_gemm<T>(m, qn, pl.b, mx.K_all + pq, mx.E_all + pq * pl.b, mx.ldE, Bg, qn, Res, qn,
                                            s);
             }
-            if (rc) break;
+            if (r2) return r2;
             LNC_CUDA(cudaMemsetAsync(stats, 0, 16, s));
-            rc = refine_apply<T>(rank, qn, piv_row, d_nc, Res, R, n, stats, s);
-            if (rc) break;
+            r2 = refine_apply<T>(rank, qn, piv_row, d_nc, Res, R, n, stats, s, apply);
+            if (r2) return r2;
             unsigned long long hs[2];
             LNC_CUDA(cudaMemcpyAsync(hs, stats, 16, cudaMemcpyDeviceToHost, s));
             LNC_CUDA(cudaStreamSynchronize(s));
-            double corr, ymax;
-            memcpy(&corr, &hs[0], 8);
-            memcpy(&ymax, &hs[1], 8);
+            memcpy(corr, &hs[0], 8);
+            memcpy(ymax, &hs[1], 8);
+            return LNC_OK;
+        };
+        double prev = INFINITY;
+        for (int it = 0; it < 10 && !rc; ++it) {
+            double corr = 0.0, ymax = 0.0;
+            rc = correction(true, &corr, &ymax);
+            if (rc) break;
             t_mixed.iterations = it + 1;
             t_mixed.last_correction = ymax > 0 ? corr / ymax : corr;
             if (corr <= 4.0 * 1.1102230246251565e-16 * ymax || corr >= 0.5 * prev) break;
             prev = corr;
+        }
+        if (!rc) {  // a-posteriori estimate of the remaining error: one further correction, not applied
+            double corr = 0.0, ymax = 0.0;
+            rc = correction(false, &corr, &ymax);
+            t_mixed.error_estimate = ymax > 0 ? corr / ymax : corr;
         }
         cudaFreeAsync(rb, s);
         if (rc) return fail(rc);
@@ -1274,6 +1290,8 @@ int mixed_report(int* iterations, double* last_correction, int* redone) {
     if (redone) *redone = t_mixed.redone;
     return LNC_OK;
 }
+
+double mixed_error_estimate() { return t_mixed.error_estimate; }
 
 // device scratch one (out-of-place) solve allocates, 0 when the shape is not supported
 size_t rref_device_scratch(int dtype, int64_t m, int64_t n) {
@@ -1320,10 +1338,13 @@ int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol
 // The array's name in host code is only a host-side stand-in; the device
 // address is obtained once per device with cudaGetSymbolAddress, on that
 // device's first call of lnc_rref_device_noalloc (so make that first call
-// before any stream capture).  All calls share the array and it keeps the
-// previous call's contents; rref_run clears everything that must start at
-// zero.  Calls that overlap on the GPU (concurrent streams, or devices not
-// yet synchronised between calls) race on the array.
+// before any stream capture), and kept for the life of the process: like the
+// library's other per-device state it does not survive cudaDeviceReset.  All
+// calls share the array and it keeps the previous call's contents; rref_run
+// clears everything that must start at zero.  Calls that overlap on the GPU
+// (concurrent streams, or devices not yet synchronised between calls) race on
+// the array.  Input and output must not overlap at all: the final row gather
+// reads the work matrix while it writes the output.
 // ----------------------------------------------------------------------------
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -1346,6 +1367,12 @@ static int noalloc_scratch(void** out) {
     return LNC_OK;
 }
 
+// [a, a + bytes_a) and [b, b + bytes_b) share at least one byte
+static bool ranges_overlap(const void* a, size_t bytes_a, const void* b, size_t bytes_b) {
+    const uintptr_t a0 = (uintptr_t)a, b0 = (uintptr_t)b;
+    return a0 < b0 + bytes_b && b0 < a0 + bytes_a;
+}
+
 template <class F>
 static int rref_noalloc_typed(const F& f, void* work, int64_t ldw, void* out, int64_t ldo, int64_t m, int64_t n,
                               int64_t* dev_piv, int64_t* dev_rank, cudaStream_t s, int flags) {
@@ -1360,6 +1387,12 @@ static int rref_noalloc_typed(const F& f, void* work, int64_t ldw, void* out, in
                   (long long)m, (long long)n, need, kNoAllocScratchBytes);
         return LNC_ERR_INVALID;
     }
+    const size_t work_bytes = sizeof(T) * ((size_t)ldw * (size_t)(m - 1) + (size_t)n);
+    const size_t out_bytes = sizeof(T) * ((size_t)ldo * (size_t)(m - 1) + (size_t)n);
+    if (ranges_overlap(work, work_bytes, out, out_bytes)) {
+        set_error("the no-allocation RREF needs input and output buffers that do not overlap");
+        return LNC_ERR_INVALID;
+    }
     void* scratch = nullptr;
     rc = noalloc_scratch(&scratch);
     if (rc) return rc;
@@ -1369,10 +1402,6 @@ static int rref_noalloc_typed(const F& f, void* work, int64_t ldw, void* out, in
 int rref_device_noalloc_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol, void* work,
                                  int64_t ldw, void* out, int64_t ldo, int64_t* dev_piv, int64_t* dev_rank,
                                  cudaStream_t s, int flags) {
-    if (out == work) {
-        set_error("the no-allocation RREF needs distinct input and output buffers");
-        return LNC_ERR_INVALID;
-    }
     switch (dtype) {
         case LNC_U32: return rref_noalloc_typed(FieldU32::make(p), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);
         case LNC_U64: return rref_noalloc_typed(FieldU64::make(p), work, ldw, out, ldo, m, n, dev_piv, dev_rank, s, flags);

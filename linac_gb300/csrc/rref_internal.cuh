@@ -257,7 +257,7 @@ int refine_build_z(int64_t n, int q, const int32_t* colmap, const int32_t* Nc, c
                    cudaStream_t s);
 template <class T>
 int refine_apply(int64_t rank, int q, const int32_t* piv_row, const int32_t* Nc, const T* D, T* R, int64_t ldr,
-                 unsigned long long* stats, cudaStream_t s);
+                 unsigned long long* stats, cudaStream_t s, bool apply = true);
 
 template <class F>
 inline int trailing_update(const TrailingCtx<F>& t, cudaStream_t s) {
@@ -279,5 +279,6 @@ int rref_device_dispatch(int dtype, int64_t m, int64_t n, uint64_t p, double tol
 int rref_read_and_clear_status(int* status);
 size_t rref_device_scratch(int dtype, int64_t m, int64_t n);
 int mixed_report(int* iterations, double* last_correction, int* redone);
+double mixed_error_estimate();
 
 }  // namespace lnc

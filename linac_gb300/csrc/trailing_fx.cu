@@ -320,7 +320,8 @@ static __global__ void build_z_kernel(int64_t n, int q, const int32_t* colmap, c
 // (non-negative doubles compare like their bit patterns)
 template <class T>
 static __global__ void apply_correction_kernel(int64_t rank, int q, const int32_t* piv_row, const int32_t* Nc,
-                                               const T* D, T* R, int64_t ldr, unsigned long long* stats) {
+                                               const T* D, T* R, int64_t ldr, unsigned long long* stats,
+                                               int apply) {
     double mc = 0.0, mv = 0.0;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < rank * q;
          idx += (int64_t)gridDim.x * blockDim.x) {
@@ -328,7 +329,7 @@ static __global__ void apply_correction_kernel(int64_t rank, int q, const int32_
         const int j = (int)(idx % q);
         const T corr = D[(int64_t)piv_row[t] * q + j];
         T* y = R + t * ldr + Nc[j];
-        *y = Ar<T>::add(*y, corr);
+        if (apply) *y = Ar<T>::add(*y, corr);
         mc = fmax(mc, Ar<T>::absv(corr));
         mv = fmax(mv, Ar<T>::absv(*y));
     }
@@ -366,9 +367,9 @@ int refine_build_z(int64_t n, int q, const int32_t* colmap, const int32_t* Nc, c
 
 template <class T>
 int refine_apply(int64_t rank, int q, const int32_t* piv_row, const int32_t* Nc, const T* D, T* R, int64_t ldr,
-                 unsigned long long* stats, cudaStream_t s) {
+                 unsigned long long* stats, cudaStream_t s, bool apply) {
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((rank * q + 255) / 256, 4096));
-    fx::apply_correction_kernel<T><<<grid, 256, 0, s>>>(rank, q, piv_row, Nc, D, R, ldr, stats);
+    fx::apply_correction_kernel<T><<<grid, 256, 0, s>>>(rank, q, piv_row, Nc, D, R, ldr, stats, apply ? 1 : 0);
     LNC_CHECK_LAUNCH("apply_correction_kernel");
     return LNC_OK;
 }
@@ -382,8 +383,8 @@ template int refine_build_z<double>(int64_t, int, const int32_t*, const int32_t*
 template int refine_build_z<c128>(int64_t, int, const int32_t*, const int32_t*, const c128*, int64_t, c128*,
                                   cudaStream_t);
 template int refine_apply<double>(int64_t, int, const int32_t*, const int32_t*, const double*, double*, int64_t,
-                                  unsigned long long*, cudaStream_t);
+                                  unsigned long long*, cudaStream_t, bool);
 template int refine_apply<c128>(int64_t, int, const int32_t*, const int32_t*, const c128*, c128*, int64_t,
-                                unsigned long long*, cudaStream_t);
+                                unsigned long long*, cudaStream_t, bool);
 
 }  // namespace lnc

@@ -63,6 +63,8 @@ def _load():
             lib.oracle_load_f64.argtypes = [vp, i64, i64, vp, i64, i64, vp]
             lib.oracle_load_c128.argtypes = [vp, i64, i64, vp, i64, i64, vp]
             lib.oracle_matmul_modp.argtypes = [vp, vp, i64, i64, i64, u64, vp, cint]
+            lib.oracle_residual_f64.argtypes = [vp, vp, vp, i64, i64, i64, vp, cint]
+            lib.oracle_residual_c128.argtypes = [vp, vp, vp, i64, i64, i64, vp, cint]
             _lib = lib
     return _lib
 
@@ -162,3 +164,41 @@ def matmul_modp(B, C, p: int, nthreads: int | None = None):
     lib.oracle_matmul_modp(B.ctypes.data, C.ctypes.data, m, k, n, int(p), out.ctypes.data,
                            nthreads or default_threads())
     return out
+
+
+def residual_dd(A, X, B, nthreads: int | None = None):
+    """B - A X with double-double accumulation, rounded once (float64 or
+    complex128 operands)."""
+    lib = _load()
+    cplx = np.iscomplexobj(A) or np.iscomplexobj(X) or np.iscomplexobj(B)
+    dt = np.complex128 if cplx else np.float64
+    A = np.ascontiguousarray(A, dtype=dt)
+    X = np.ascontiguousarray(X, dtype=dt)
+    B = np.ascontiguousarray(B, dtype=dt)
+    m, k = A.shape
+    q = X.shape[1]
+    assert X.shape[0] == k and B.shape == (m, q)
+    out = np.empty((m, q), dtype=dt)
+    f = lib.oracle_residual_c128 if cplx else lib.oracle_residual_f64
+    f(A.ctypes.data, X.ctypes.data, B.ctypes.data, m, k, q, out.ctypes.data, nthreads or default_threads())
+    return out
+
+
+def reference_solution(A, B, iterations: int = 3):
+    """Solution of A X = B to FP64 accuracy: LAPACK's solve refined with
+    double-double residuals (the exact solution of the stored system, rounded;
+    cond(A) * eps^2 below FP64's own rounding for cond(A) << 1/eps)."""
+    try:
+        from scipy.linalg import lu_factor, lu_solve
+    except ImportError:  # one factorisation per solve without scipy
+        def solve(rhs):
+            return np.linalg.solve(A, rhs)
+    else:
+        lu = lu_factor(A)
+
+        def solve(rhs):
+            return lu_solve(lu, rhs)
+    X = solve(B)
+    for _ in range(iterations):
+        X = X + solve(residual_dd(A, X, B))
+    return X

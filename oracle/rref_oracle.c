@@ -336,3 +336,76 @@ void oracle_matmul_modp(const uint64_t *B, const uint64_t *C, int64_t m, int64_t
         }
     }
 }
+
+/* ------------------------------------------------------------------ */
+/* Reference solutions of float systems (tests only)                   */
+/* ------------------------------------------------------------------ */
+/* out = B - A X (A m x k, X k x q, B and out m x q; row-major, real or
+ * complex as interleaved pairs) with every product split exactly by fma
+ * (Dekker/Kahan TwoProduct) and every sum carried in double-double (Knuth's
+ * TwoSum), rounded once at the end.  Iterating X += A^-1 (B - A X) with this
+ * residual converges to the exact solution of the stored system to FP64
+ * accuracy (Wilkinson's refinement with an extended-precision residual);
+ * the tests compare the mixed-precision GPU result against that solution.
+ * The explicit fma calls are unaffected by -ffp-contract=off. */
+static inline void two_sum(double a, double b, double *s, double *e) {
+    double x = a + b, bv = x - a;
+    *e = (a - (x - bv)) + (b - bv);
+    *s = x;
+}
+
+static inline void dd_acc(double *hi, double *lo, double p, double pe) {
+    double s, e;
+    two_sum(*hi, p, &s, &e);
+    *hi = s;
+    *lo += e + pe;
+}
+
+void oracle_residual_f64(const double *A, const double *X, const double *B, int64_t m, int64_t k, int64_t q,
+                         double *out, int nthreads) {
+    #pragma omp parallel for schedule(static) num_threads(nthreads) if(nthreads > 1)
+    for (int64_t r = 0; r < m; ++r) {
+        double *hi = (double *)malloc(sizeof(double) * (size_t)(2 * q));
+        double *lo = hi + q;
+        for (int64_t c = 0; c < q; ++c) { hi[c] = B[r * q + c]; lo[c] = 0.0; }
+        for (int64_t t = 0; t < k; ++t) {
+            const double a = -A[r * k + t];
+            if (a == 0.0) continue;
+            for (int64_t c = 0; c < q; ++c) {
+                const double x = X[t * q + c], p = a * x;
+                dd_acc(&hi[c], &lo[c], p, fma(a, x, -p));
+            }
+        }
+        for (int64_t c = 0; c < q; ++c) out[r * q + c] = hi[c] + lo[c];
+        free(hi);
+    }
+}
+
+void oracle_residual_c128(const double *A, const double *X, const double *B, int64_t m, int64_t k, int64_t q,
+                          double *out, int nthreads) {
+    #pragma omp parallel for schedule(static) num_threads(nthreads) if(nthreads > 1)
+    for (int64_t r = 0; r < m; ++r) {
+        double *acc = (double *)malloc(sizeof(double) * (size_t)(4 * q));  /* re hi, re lo, im hi, im lo */
+        for (int64_t c = 0; c < q; ++c) {
+            acc[4 * c] = B[2 * (r * q + c)]; acc[4 * c + 1] = 0.0;
+            acc[4 * c + 2] = B[2 * (r * q + c) + 1]; acc[4 * c + 3] = 0.0;
+        }
+        for (int64_t t = 0; t < k; ++t) {
+            const double ar = -A[2 * (r * k + t)], ai = -A[2 * (r * k + t) + 1];
+            if (ar == 0.0 && ai == 0.0) continue;
+            for (int64_t c = 0; c < q; ++c) {
+                const double xr = X[2 * (t * q + c)], xi = X[2 * (t * q + c) + 1];
+                double p;
+                p = ar * xr; dd_acc(&acc[4 * c], &acc[4 * c + 1], p, fma(ar, xr, -p));
+                p = -(ai * xi); dd_acc(&acc[4 * c], &acc[4 * c + 1], p, fma(-ai, xi, -p));
+                p = ar * xi; dd_acc(&acc[4 * c + 2], &acc[4 * c + 3], p, fma(ar, xi, -p));
+                p = ai * xr; dd_acc(&acc[4 * c + 2], &acc[4 * c + 3], p, fma(ai, xr, -p));
+            }
+        }
+        for (int64_t c = 0; c < q; ++c) {
+            out[2 * (r * q + c)] = acc[4 * c] + acc[4 * c + 1];
+            out[2 * (r * q + c) + 1] = acc[4 * c + 2] + acc[4 * c + 3];
+        }
+        free(acc);
+    }
+}

@@ -1,9 +1,16 @@
 """Mixed-precision float RREF (LNC_FLAG_MIXED): fixed-point tensor-core
-trailing updates, FP64 panels, FP64 refinement.  The result must agree with
-the FP64 oracle (linac's row_reduce restated in C, pivoting=1, scaling=True,
-threshold 1e-9) within 1e-10 in the max norm relative to the result's largest
-entry, take the same pivot columns, and be at least as close to the exact
-solution as the oracle is."""
+trailing updates, FP64 panels, FP64 refinement.
+
+The bound is 1e-10 in the max norm relative to the result's largest entry.
+Small systems are held to it against the FP64 oracle (linac's row_reduce
+restated in C, pivoting=1, scaling=True, threshold 1e-9), with the same pivot
+columns.  At the benchmark's sizes (2,000 and 5,000 unknowns, condition 1e6)
+the FP64 oracle is itself about cond * eps ~ 1e-10 away from the exact
+solution, so no result more accurate than the oracle can be within 1e-10 of
+it; there the bound is held against the FP64-accurate reference solution of
+the stored system (LAPACK refined with double-double residuals,
+oracle.reference_solution), and the result's own error estimate
+(mixed_report()["error_estimate"]) must be within it as well."""
 import numpy as np
 import pytest
 
@@ -21,13 +28,8 @@ def _rel(a, b):
 
 
 def _truth(A, B):
-    """A^-1 B refined with an extended-precision residual (reference answer)."""
-    X = np.linalg.solve(A, B)
-    Al = A.astype(np.clongdouble if np.iscomplexobj(A) else np.longdouble)
-    for _ in range(3):
-        r = (B - (Al @ X.astype(Al.dtype))).astype(A.dtype)
-        X = X + np.linalg.solve(A, r)
-    return X
+    """A^-1 B to FP64 accuracy (refined with double-double residuals)."""
+    return oracle.reference_solution(A, B)
 
 
 @pytest.mark.parametrize("n,cplx", [(300, False), (700, False), (257, True), (500, True)])
@@ -86,3 +88,25 @@ def test_rank_deficient_is_redone_in_fp64():
 def test_mixed_rejects_prime_fields():
     with pytest.raises(ValueError):
         cuda_row_reduce(np.eye(3, dtype=np.uint32), 7, mixed=True)
+
+
+@pytest.mark.parametrize("n,cplx", [(2000, False), (2000, True), (5000, False), (5000, True)])
+def test_benchmark_sizes_within_bound_of_reference_solution(n, cplx):
+    """[A | B] with A = U diag(s) V^H (cond 1e6) and 16 right-hand sides, as
+    the float benchmark: the solution block within 1e-10 of the reference
+    solution, the pivot block exactly I, the per-result error estimate within
+    the bound and of the order of the measured error."""
+    rng = np.random.default_rng(5000 + n + cplx)
+    A = workloads.conditioned_matrix(n, rng, cond=1e6, complex_=cplx)
+    B = rng.standard_normal((n, 16)) + (1j * rng.standard_normal((n, 16)) if cplx else 0)
+    M = np.hstack([A, B])
+    R, piv = cuda_row_reduce(M, 0, return_pivots=True, mixed=True)
+    rep = _lib.mixed_report()
+    assert piv == list(range(n)) and not rep["redone_fp64"]
+    assert np.array_equal(R[:, :n], np.eye(n))
+    X = _truth(A, B)
+    err = _rel(R[:, n:], X)
+    assert err <= TOL, (err, rep)
+    est = rep["error_estimate"]
+    assert est is not None and est <= TOL, rep
+    assert err <= 20.0 * est + 1e-14, (err, est)

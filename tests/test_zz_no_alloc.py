@@ -7,7 +7,9 @@ point: its scratch is a fixed 16 MiB array inside the library, not
 stream-ordered allocations.  These tests check, through the C ABI, that it
 returns exactly what the allocating entry point (lnc_rref_device) returns, on
 two calls in a row (the second call reuses the array the first one left
-dirty), and that a request too large for the fixed array is refused.
+dirty), that both agree with the CPU oracle (so a scratch-layout fault the two
+entry points share would not pass), and that a request too large for the
+fixed array, or with overlapping input and output, is refused.
 
 This file is named so that pytest collects it last; it is self-contained and
 passes on its own in a fresh process as well as after the other tests.
@@ -17,6 +19,7 @@ import ctypes
 import numpy as np
 import pytest
 
+import oracle
 from linac_gb300 import _lib, workloads
 
 pytestmark = pytest.mark.gpu
@@ -67,6 +70,9 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls():
         assert rank == rank_ref
         assert np.array_equal(piv, piv_ref)
         assert np.array_equal(R, R_ref)
+        R_o, piv_o, rank_o = oracle.rref_modp(A, p)
+        assert rank == rank_o and list(piv[:rank]) == list(piv_o)
+        assert np.array_equal(R.astype(np.uint64), R_o)
 
 
 def test_noalloc_float_matches_allocating_entry_point():
@@ -83,6 +89,10 @@ def test_noalloc_float_matches_allocating_entry_point():
     assert rank == rank_ref and np.array_equal(piv, piv_ref)
     # same kernels on the same inputs: agreement to 1e-12 (the float tests' bar is 1e-9)
     assert np.allclose(R, R_ref, rtol=0, atol=1e-12)
+    # and the FP64 oracle (linac's CPU row_reduce, pivoting=1, scaling=True): the float tests' 1e-9
+    R_o, piv_o, rank_o = oracle.rref_f64(A)
+    assert rank == rank_o and list(piv[:rank]) == list(piv_o)
+    assert np.allclose(R, R_o, rtol=1e-9, atol=1e-9)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
@@ -96,3 +106,7 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     assert "no-allocation scratch" in _lib.last_error()
     rc = noalloc(_lib.LNC_U32, 10, 10, 2**31 - 1, 0.0, dummy.ptr, 10, dummy.ptr, 10, None, None, None, 0)
     assert rc == _lib.LNC_ERR_INVALID  # in place is refused: output must be a separate buffer
+    assert "do not overlap" in _lib.last_error()
+    # a partial overlap (the output starts inside the input) is refused as well
+    rc = noalloc(_lib.LNC_U32, 2, 2, 2**31 - 1, 0.0, dummy.ptr, 2, dummy.ptr + 8, 2, None, None, None, 0)
+    assert rc == _lib.LNC_ERR_INVALID and "do not overlap" in _lib.last_error()

@@ -542,12 +542,16 @@ static int plan_create(const lnc_batch_matrix* mats, int64_t count, int tpc, int
     }
     // ---- capture the whole batch into one graph
     const size_t cand_smem = (size_t)(P->smax | 1) * kMaxPanel * 4 + 2 * kMaxPanel * 4 + 256 * 4;
-    LNC_CUDA(cudaFuncSetAttribute(batch_cand_kernel<ArithSmall, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)cand_smem));
-    LNC_CUDA(cudaFuncSetAttribute(batch_cand_kernel<ArithMont, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)cand_smem));
-    LNC_CUDA(cudaFuncSetAttribute(batch_cand_kernel<ArithTwo, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)cand_smem));
+    for (const void* k : {(const void*)batch_cand_kernel<ArithSmall, 1>, (const void*)batch_cand_kernel<ArithMont, 2>,
+                          (const void*)batch_cand_kernel<ArithTwo, 0>}) {
+        const int rc0 = allow_dynamic_smem(k, cand_smem);
+        if (rc0) {
+            cudaFreeAsync(P->d_desc, s);
+            cudaFreeAsync(P->arena, s);
+            delete P;
+            return rc0;
+        }
+    }
     LNC_CUDA(cudaFuncSetAttribute(batch_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES));
     LNC_CUDA(cudaStreamSynchronize(s));
     cudaStream_t cs;

@@ -70,7 +70,8 @@ static int launch_cand_cluster(const CandArgs& a, double elt, cudaStream_t s) {
 
 template <class Arith>
 static int launch_cand_typed(const CandArgs& a, size_t smem, cudaStream_t s) {
-    LNC_CUDA(cudaFuncSetAttribute(cand_panel_kernel<Arith>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int rc = allow_dynamic_smem((const void*)cand_panel_kernel<Arith>, smem);
+    if (rc) return rc;
     ScopedKernelTimer kt(KC_PANEL, s, 2.0 * a.smax * a.bw * 4.0);
     cand_panel_kernel<Arith><<<1, kCandThreads, smem, s>>>(a);
     LNC_CHECK_LAUNCH("cand_panel_kernel");
@@ -101,7 +102,8 @@ int launch_cand_panel64(const CandArgs& a, cudaStream_t s) {
     if (cl == 4) return launch_cand_cluster<Arith64, uint64_t, kPanelU64, 4>(a, 8.0, s);
     const size_t smem = cand_smem<uint64_t, kPanelU64>(a.smax);
     auto kern = cand_panel_kernel<Arith64, uint64_t, kPanelU64>;
-    LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int rc = allow_dynamic_smem((const void*)kern, smem);
+    if (rc) return rc;
     ScopedKernelTimer kt(KC_PANEL, s, 2.0 * a.smax * a.bw * 8.0);
     kern<<<1, kCandThreads, smem, s>>>(a);
     LNC_CHECK_LAUNCH("cand_panel_kernel (64-bit)");

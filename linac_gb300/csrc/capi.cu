@@ -123,6 +123,32 @@ int device_info(DeviceInfo* out) {
     return LNC_OK;
 }
 
+static std::mutex g_smem_mu;
+static std::vector<std::pair<const void*, int>> g_smem_done;  // (kernel, device) pairs already raised
+
+int allow_dynamic_smem(const void* kernel, size_t need) {
+    DeviceInfo di;
+    int rc = device_info(&di);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> g(g_smem_mu);
+    for (const auto& kd : g_smem_done)
+        if (kd.first == kernel && kd.second == di.device) {
+            return need <= (size_t)di.smem_optin ? LNC_OK
+                                                  : (set_error("kernel needs %zu bytes of shared memory", need),
+                                                     LNC_ERR_UNSUPPORTED);
+        }
+    cudaFuncAttributes fa;
+    LNC_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    const size_t cap = (size_t)di.smem_optin - fa.sharedSizeBytes;
+    if (need > cap) {
+        set_error("kernel needs %zu bytes of dynamic shared memory; the device allows %zu", need, cap);
+        return LNC_ERR_UNSUPPORTED;
+    }
+    LNC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+    g_smem_done.emplace_back(kernel, di.device);
+    return LNC_OK;
+}
+
 // Per-thread library stream (non-blocking), created on first use per device.
 static thread_local cudaStream_t t_streams[64] = {nullptr};
 static int library_stream(cudaStream_t* s) {

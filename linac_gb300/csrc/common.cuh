@@ -64,6 +64,13 @@ struct DeviceInfo {
 };
 int device_info(DeviceInfo* out);
 
+// Raise a kernel's dynamic shared-memory limit to everything the device allows
+// beside its static shared memory (once per kernel and device), and check that
+// `need` bytes fit.  The limit is a property of the kernel, shared by all host
+// threads: setting it to each launch's own size would let a concurrent launch
+// with a larger size on another thread fail.
+int allow_dynamic_smem(const void* kernel, size_t need);
+
 size_t dtype_size(int dtype);
 bool is_prime_u64(uint64_t n);
 int validate_rref_args(int dtype, int64_t m, int64_t n, uint64_t p, int64_t ld);

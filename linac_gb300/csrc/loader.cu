@@ -331,7 +331,8 @@ static int launch_loader(const Ops& ops, int64_t n_rows, int64_t n_cols, int64_t
         return LNC_ERR_UNSUPPORTED;
     }
     auto kern = load_matrix_kernel<Ops, ROWS>;
-    LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    rc = allow_dynamic_smem((const void*)kern, smem);
+    if (rc) return rc;
     dim3 grid;
     rc = loader_grid(n_rows, n_cols, ROWS, &grid);
     if (rc) return rc;
@@ -353,9 +354,10 @@ static int launch_pairs(uint64_t p, int64_t n_rows, int64_t n_cols, int64_t basi
                         const void* bases, const uint32_t* lind, void* out, int64_t ldo, int* status, cudaStream_t s) {
     const size_t smem = pairs_smem(basis_len, degree);
     auto kern = load_pairs_kernel<kPairRows>;
-    LNC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int rc = allow_dynamic_smem((const void*)kern, smem);
+    if (rc) return rc;
     dim3 grid;
-    int rc = loader_grid(n_rows, n_cols, kPairRows, &grid);
+    rc = loader_grid(n_rows, n_cols, kPairRows, &grid);
     if (rc) return rc;
     ScopedKernelTimer kt(KC_LOADER, s, loader_bytes(4, n_rows, n_cols, basis_len, degree));
     kern<<<grid, kLoadCols, smem, s>>>(ShoupPairs::make(p), (const uint32_t*)bases, (int)n_rows, (int)basis_len, lind,

@@ -709,7 +709,10 @@ int rref_run(const F& f, typename F::T* A, int64_t m, int64_t n, int64_t lda, ty
 
     auto kpanel = panel_kernel<F>;
     const size_t smem_max = panel_smem_bytes<F>(pl.rows_per_cta, pl.b);
-    LNC_CUDA(cudaFuncSetAttribute(kpanel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+    {
+        int rc0 = allow_dynamic_smem((const void*)kpanel, smem_max);
+        if (rc0) return rc0;
+    }
 
     TrailingCtx<F> tctx;
     tctx.f = f;

@@ -107,6 +107,7 @@ def test_benchmark_sizes_within_bound_of_reference_solution(n, cplx):
     X = _truth(A, B)
     err = _rel(R[:, n:], X)
     assert err <= TOL, (err, rep)
+    # the estimate (one further FP64-residual correction) is of the order of the error: at
+    # condition 1e6 both sit at the FP64 floor cond * eps, the estimate somewhat above
     est = rep["error_estimate"]
-    assert est is not None and est <= TOL, rep
-    assert err <= 20.0 * est + 1e-14, (err, est)
+    assert est is not None and est / 4.0 <= err + 1e-15 and err <= 4.0 * est, (err, est)

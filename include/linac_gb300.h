@@ -170,7 +170,7 @@ int lnc_rref_device_noalloc(int dtype, int64_t m, int64_t n, uint64_t p, double 
 
 /* ---- batched RREF (many uneven matrices, a prime each) ---------------------- */
 typedef struct lnc_batch_matrix {
-    uint64_t p;             /* prime, < 2^32 */
+    uint64_t p;             /* prime: < 2^32 for LNC_U32, any for LNC_U64, ignored for floats */
     int64_t m, n;
     const void* dev_in;     /* m x n input (not modified), leading dimension ld_in */
     int64_t ld_in;
@@ -200,7 +200,10 @@ int lnc_batch_plan_finish(void* plan, void* stream, int64_t* n_redo);
 /* Device bytes held by the plan (admission accounting). */
 int64_t lnc_batch_plan_bytes(void* plan);
 int lnc_batch_plan_destroy(void* plan);
-/* create + run + finish + destroy */
+/* LNC_U32: create + run + finish + destroy.  LNC_U64 (a prime per matrix, up
+ * to 2^64 - 59; no captured plan): every matrix through the single-matrix
+ * 64-bit path, on 8 worker threads with their own streams, after the work
+ * already queued on `stream`; synchronous.  Inputs are not modified. */
 int lnc_rref_batch_device(int dtype, const lnc_batch_matrix* mats, int64_t count, void* stream, int flags);
 
 /* ---- batched float / complex RREF --------------------------------------------- */

@@ -159,15 +159,44 @@ class BatchPlan:
             pass
 
 
-def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True):
-    """RREF of every matrix of the list over F_{primes[i]} (uint32 residues).
+def _residues_u64(A: np.ndarray, q: int) -> np.ndarray:
+    """Entries of A reduced to [0, q) as uint64 (integer or object arrays)."""
+    if A.dtype == object:
+        return np.vectorize(lambda x: int(x) % q, otypes=[object])(A).astype(np.uint64)
+    if A.dtype.kind == "u":
+        return A.astype(np.uint64) % np.uint64(q)
+    if A.dtype.kind != "i":
+        raise TypeError("F_p batches take integer matrices")
+    a = A.astype(np.int64)
+    if q < 2**63:
+        return np.mod(a, np.int64(q)).astype(np.uint64)
+    # q > |a|: a mod q is a, or a + q for a negative a (two's complement wraps to it)
+    return a.view(np.uint64) + (a < 0).astype(np.uint64) * np.uint64(q)
 
-    Returns the list of RREFs (uint32 arrays), and the pivot columns when
-    ``return_pivots``.  One plan (one CUDA graph) covers the whole list.
+
+def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True):
+    """RREF of every matrix of the list over F_{primes[i]}.
+
+    Returns the list of RREFs, and the pivot columns when ``return_pivots``.
+    With every prime below 2^32 the residues are uint32 and one plan (one CUDA
+    graph) covers the whole list; with any prime above, every matrix is
+    reduced as uint64 residues (linac's dtype rule,
+    linac/pycuda_row_reduce.py:41-46) through the single-matrix 64-bit path
+    on concurrent worker streams.
     """
     mats = [np.asarray(A) for A in matrices]
     if isinstance(primes, (int, np.integer)):
         primes = [int(primes)] * len(mats)
+    if any(int(q) > 2**32 - 1 for q in primes):
+        cb = ConcurrentBatch([A.shape for A in mats], np.uint64, primes)
+        packed = cb.pack([_residues_u64(A, int(q)) for A, q in zip(mats, primes)])
+        cb.upload(packed)
+        cb.run()
+        res = [R.copy() for R in cb.unpack(cb.download())]
+        if return_pivots:
+            pivs, _ = cb.pivots_and_ranks()
+            return res, [[int(x) for x in p] for p in pivs]
+        return res
     shapes = [A.shape for A in mats]
     tpc, cand = autotune(shapes, primes) if tune else (0, 0)
     plan = BatchPlan(shapes, primes, tpc, cand)
@@ -186,16 +215,31 @@ def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True)
         plan.close()
 
 
-class FloatBatch:
-    """Device buffers for a list of float64 / complex128 matrices (inputs and
-    outputs packed, 256-byte aligned) and the descriptors of
-    lnc_rref_float_batch; ``run`` solves them all."""
+class ConcurrentBatch:
+    """Device buffers for a list of matrices (inputs and outputs packed,
+    256-byte aligned) and their descriptors; ``run`` solves them all, each
+    through the single-matrix path, on concurrent worker streams.
 
-    def __init__(self, shapes, dtype):
+    float64 / complex128 batches go to lnc_rref_float_batch; uint64 batches
+    (64-bit residues, ``primes[i]`` per matrix) to lnc_rref_batch_device."""
+
+    DTYPES = (np.dtype(np.float64), np.dtype(np.complex128), np.dtype(np.uint64))
+
+    def __init__(self, shapes, dtype, primes=None):
         _bind()
         self.dtype = np.dtype(dtype)
-        if self.dtype not in (np.dtype(np.float64), np.dtype(np.complex128)):
-            raise ValueError("float batches hold float64 or complex128 matrices")
+        if self.dtype not in self.DTYPES:
+            raise ValueError(f"{type(self).__name__} holds {', '.join(str(d) for d in self.DTYPES)} matrices")
+        self.modp = self.dtype == np.dtype(np.uint64)
+        if self.modp:
+            if primes is None:
+                raise ValueError("a uint64 batch needs a prime per matrix")
+            primes = [int(primes)] * len(shapes) if isinstance(primes, (int, np.integer)) else [int(q) for q in primes]
+            if len(primes) != len(shapes):
+                raise ValueError("one prime per matrix")
+            for q in primes:
+                check_prime(q)
+        self.primes = primes
         self.code = _lib.DTYPE_CODE[self.dtype]
         self.shapes = [(int(m), int(n)) for m, n in shapes]
         elt = self.dtype.itemsize
@@ -213,7 +257,7 @@ class FloatBatch:
         descs = (lnc_batch_matrix * max(1, len(self.shapes)))()
         for i, (m, n) in enumerate(self.shapes):
             d = descs[i]
-            d.p, d.m, d.n = 0, m, n
+            d.p, d.m, d.n = (self.primes[i] if self.modp else 0), m, n
             d.dev_in = self.d_in.ptr + self.offsets[i]
             d.ld_in = n
             d.dev_out = self.d_out.ptr + self.offsets[i]
@@ -234,6 +278,10 @@ class FloatBatch:
         _lib.check(_lib.lib().lnc_stream_synchronize(stream))
 
     def run(self, mixed: bool = True, workers: int = 8, tol: float = 1e-9):
+        if self.modp:
+            _lib.check(_lib.lib().lnc_rref_batch_device(self.code, ctypes.addressof(self._descs), len(self.shapes),
+                                                        None, 0), "lnc_rref_batch_device")
+            return
         flags = _lib.LNC_FLAG_MIXED if mixed else 0
         _lib.check(_lib.lib().lnc_rref_float_batch(self.code, ctypes.addressof(self._descs), len(self.shapes),
                                                    float(tol), flags, int(workers),
@@ -261,6 +309,15 @@ class FloatBatch:
         return [{"iterations": r.iterations, "redone_fp64": bool(r.redone_fp64),
                  "error_estimate": None if r.redone_fp64 else r.error_estimate}
                 for r in self.reports[:len(self.shapes)]]
+
+
+class FloatBatch(ConcurrentBatch):
+    """A ConcurrentBatch of float64 / complex128 matrices."""
+
+    DTYPES = (np.dtype(np.float64), np.dtype(np.complex128))
+
+    def __init__(self, shapes, dtype):
+        super().__init__(shapes, dtype)
 
 
 def rref_float_batch(matrices, mixed: bool = True, workers: int = 8, return_pivots: bool = False,

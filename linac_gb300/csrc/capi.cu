@@ -1,12 +1,15 @@
 // C ABI of liblinac_gb300 (declared in include/linac_gb300.h) and the shared
 // host-side helpers: error messages, launch counting, kernel timing, device
 // properties and the per-thread library stream.
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <unistd.h>
 #include <vector>
 
 #include "common.cuh"
@@ -158,6 +161,66 @@ static int library_stream(cudaStream_t* s) {
     *s = t_streams[dev];
     return LNC_OK;
 }
+
+// ---- first touch of pageable host destinations -----------------------------
+// A device-to-host copy into pageable memory that has never been written (a
+// fresh numpy or malloc array) maps the destination one page at a time inside
+// the copy: measured at about 1 s per GB on a Grace host, ten times the whole
+// solve of a 20,000^2 matrix.  HostPrefault writes one zero per page of the
+// destination rows from a few host threads while the GPU works; the copy then
+// lands in mapped pages.  Pinned / registered memory and small buffers are
+// left alone, and so is a destination that overlaps the input [src, src +
+// src_bytes) (an in-place call: its pages are mapped, and the input must not
+// be overwritten before it is copied).  join() must return before the copy
+// into the buffer is queued.
+class HostPrefault {
+  public:
+    HostPrefault(void* base, size_t row_bytes, size_t pitch, int64_t rows, const void* src, size_t src_bytes) {
+        const size_t span = rows > 0 ? pitch * (size_t)(rows - 1) + row_bytes : 0;
+        if (!base || span < ((size_t)64 << 20)) return;
+        const uintptr_t b0 = (uintptr_t)base, s0 = (uintptr_t)src;
+        if (src && b0 < s0 + src_bytes && s0 < b0 + span) return;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, base) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        if (a.type != cudaMemoryTypeUnregistered) return;
+        long pg = sysconf(_SC_PAGESIZE);
+        const size_t page = pg > 0 ? (size_t)pg : 4096;
+        unsigned hc = std::thread::hardware_concurrency();
+        const bool contiguous = pitch == row_bytes || rows == 1;
+        const int64_t nt = std::max<int64_t>(
+            1, std::min<int64_t>({(int64_t)(hc ? hc / 2 : 4), 8, contiguous ? (int64_t)8 : rows}));
+        for (int64_t t = 0; t < nt; ++t) {
+            try {
+            threads_.emplace_back([=]() {
+                volatile unsigned char* b = (volatile unsigned char*)base;
+                auto touch = [&](size_t lo, size_t hi) {  // one write per page of [lo, hi)
+                    for (size_t x = lo; x < hi; x = (x / page + 1) * page) b[x] = 0;
+                };
+                if (contiguous) {
+                    const size_t chunk = (span + nt - 1) / nt;
+                    const size_t lo = chunk * t, hi = std::min(span, lo + chunk);
+                    if (lo < hi) touch(lo, hi);
+                } else {
+                    for (int64_t r = t; r < rows; r += nt) touch(pitch * (size_t)r, pitch * (size_t)r + row_bytes);
+                }
+            });
+            } catch (...) {  // no thread to spare: the pages left are mapped by the copy itself
+                break;
+            }
+        }
+    }
+    void join() {
+        for (auto& th : threads_) th.join();
+        threads_.clear();
+    }
+    ~HostPrefault() { join(); }
+
+  private:
+    std::vector<std::thread> threads_;
+};
 
 // ---- modulus validation ----------------------------------------------------
 static uint64_t mulmod_u64(uint64_t a, uint64_t b, uint64_t m) {
@@ -447,9 +510,11 @@ int lnc_rref_host(int dtype, int64_t m, int64_t n, uint64_t p, double tol, const
     }
     int64_t* dpiv = (int64_t*)dsmall;
     int64_t* drank = dpiv + kmax;
+    HostPrefault prefault(host_out, elt * n, elt * ld_out, m, host_in, elt * ((size_t)ld * (size_t)(m - 1) + (size_t)n));
     e = cudaMemcpy2DAsync(dwork, elt * n, host_in, elt * ld, elt * n, m, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) rc = cuda_status(e, "host-to-device copy");
     if (!rc) rc = rref_device_dispatch(dtype, m, n, p, tol, dwork, n, dout, n, dpiv, drank, s, flags);
+    prefault.join();
     if (!rc) {
         e = cudaMemcpy2DAsync(host_out, elt * ld_out, dout, elt * n, elt * n, m, cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess) rc = cuda_status(e, "device-to-host copy");
@@ -514,11 +579,13 @@ int lnc_load_matrix_host(int dtype, int64_t n_rows, int64_t n_cols, int64_t basi
         set_error("loader: device allocation failed: %s", cudaGetErrorString(e));
         return LNC_ERR_OOM;
     }
+    HostPrefault prefault(hout, ob, ob, 1, hbases, bb);
     if (bb) e = cudaMemcpyAsync(db, hbases, bb, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && lb) e = cudaMemcpyAsync(dl, hlind, lb, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) rc = cuda_status(e, "loader host-to-device copy");
     if (!rc) rc = load_matrix_dispatch(dtype, n_rows, n_cols, basis_len, degree, p, db, (const uint32_t*)dl, dout,
                                        n_cols, s);
+    prefault.join();
     if (!rc) {
         e = cudaMemcpyAsync(hout, dout, ob, cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess) rc = cuda_status(e, "loader device-to-host copy");
@@ -558,7 +625,14 @@ int lnc_batch_plan_destroy(void* plan) {
     return LNC_OK;
 }
 
-int lnc_rref_batch_device(int dtype, const lnc_batch_matrix* mats, int64_t count, void* stream, int /*flags*/) {
+int lnc_rref_batch_device(int dtype, const lnc_batch_matrix* mats, int64_t count, void* stream, int flags) {
+    if (dtype == LNC_U64) {
+        // no captured plan for 64-bit residues: the single-matrix path on concurrent worker streams,
+        // after the work already queued on `stream` (which may be producing the inputs)
+        if (stream) LNC_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+        return concurrent_batch(LNC_U64, mats, count, 0.0, flags & ~(LNC_FLAG_MIXED | LNC_FLAG_NO_SCALING), 0,
+                                nullptr);
+    }
     void* plan = nullptr;
     int rc = lnc_batch_plan_create(dtype, mats, count, 0, 0, stream, &plan);
     if (rc) return rc;

@@ -280,5 +280,8 @@ int rref_read_and_clear_status(int* status);
 size_t rref_device_scratch(int dtype, int64_t m, int64_t n);
 int mixed_report(int* iterations, double* last_correction, int* redone);
 double mixed_error_estimate();
+// every matrix of a batch through the single-matrix path on `workers` concurrent streams (float_batch.cu)
+int concurrent_batch(int dtype, const lnc_batch_matrix* mats, int64_t count, double tol, int flags, int workers,
+                     lnc_mixed_result* reports);
 
 }  // namespace lnc

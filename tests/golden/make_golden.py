@@ -1,7 +1,8 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference itself.
 
 Run from the repository root in a container that has the reference checkout
-(``LINAC_REFERENCE``, default /root/reference):
+(``LINAC_REFERENCE``, default: a directory ``reference`` beside the
+repository root):
 
     python tests/golden/make_golden.py
 

@@ -23,7 +23,10 @@ import sys
 import types
 from pathlib import Path
 
-REFERENCE_ROOT = Path(os.environ.get("LINAC_REFERENCE", "/root/reference"))
+# the reference checkout: $LINAC_REFERENCE, else a sibling directory named
+# "reference" next to this repository's root
+REFERENCE_ROOT = Path(os.environ.get("LINAC_REFERENCE",
+                                     Path(__file__).resolve().parents[3] / "reference"))
 
 
 def reference_available() -> bool:

@@ -94,3 +94,31 @@ def test_matmul_and_fill_helpers_exact():
     d.download(x)
     # 100000 draws from 65521 values: about 51300 distinct are expected
     assert x.max() < 65521 and 48000 < len(np.unique(x)) < 54000
+
+
+def test_u64_batch_uneven_primes_matches_oracle():
+    """64-bit residues: a prime per matrix up to 2^64 - 59, uneven and
+    rank-deficient shapes, every result against the oracle."""
+    rng = np.random.default_rng(64)
+    primes64 = [2**61 - 1, 2**64 - 59, 2**62 - 57, 4294967311]
+    mats, primes = [], []
+    for i, (m, n) in enumerate([(300, 280), (64, 900), (700, 500), (129, 129), (1, 50), (50, 1), (450, 470),
+                                (257, 300)]):
+        p = primes64[i % len(primes64)]
+        if i % 3 == 2:  # rank deficient: a product of thin factors mod p
+            r = max(1, min(m, n) // 2)
+            B = rng.integers(0, p, size=(m, r), dtype=np.uint64)
+            C = rng.integers(0, p, size=(r, n), dtype=np.uint64)
+            A = oracle.matmul_modp(B, C, p)
+        else:
+            A = rng.integers(0, p, size=(m, n), dtype=np.uint64)
+        mats.append(A)
+        primes.append(p)
+    mats.append(np.zeros((40, 30), dtype=np.uint64))
+    primes.append(2**61 - 1)
+    res, pivs = rref_batch(mats, primes, return_pivots=True)
+    for A, p, R, pv in zip(mats, primes, res, pivs):
+        R_ref, piv_ref, _ = oracle.rref_modp(A, p)
+        assert R.dtype == np.uint64
+        assert np.array_equal(R, R_ref)
+        assert pv == piv_ref

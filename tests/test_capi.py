@@ -36,7 +36,7 @@ def test_python_binding_covers_header():
     for n in header_functions():
         assert n in bound or n.startswith(("lnc_batch", "lnc_server", "lnc_serve", "lnc_tc", "lnc_autotune",
                                            "lnc_graph", "lnc_load_rref", "lnc_rref_batch", "lnc_matmul",
-                                           "lnc_rref_device_noalloc", "lnc_rref_refine")), n
+                                           "lnc_rref_device_noalloc", "lnc_rref_refine", "lnc_rref_float_batch")), n
 
 
 def test_header_constants_match_the_python_binding():

@@ -531,13 +531,19 @@ def trailing_bytes(m: int, n: int, b: int) -> float:
 
 # DRAM bytes (read + write) per launch of the dominant kernel, averaged over
 # the launches of one ncu capture of the same workload (dram__bytes_read.sum +
-# dram__bytes_write.sum, one pass): profiles/launches_rref_u32_20000.md and
-# profiles/launches_rref_u64_8000.md
+# dram__bytes_write.sum, one pass of the whole-workload launch list)
 PROFILED_TRAFFIC = {
     ("rref_u32_20000", "limb_gemm"): 322.0e6,   # look-ahead schedule: near, far and E = G X launches
     ("rref_u64_8000", "trailing_simt"): 465.4e6,
     ("rref_u64_8000", "limb_gemm"): 97.4e6,     # look-ahead schedule
 }
+
+
+# loader: DRAM bytes per algorithmic byte of one load_pairs_kernel launch
+# (8016 x 8000, degree 8 + prefactor, basis 12): 196.5 MB of ncu DRAM traffic
+# (0.92 MB read, 195.6 MB written; the last writes were still in L2 when the
+# kernel ended) for 257.2 MB of output, bases and indices
+LOADER_TRAFFIC_PER_BYTE = 196.49e6 / 257.18e6
 
 
 def traffic_per_launch(workload: str, kernel: str):
@@ -1040,10 +1046,14 @@ def run_loader(args, dist: Dist):
         "e2e": {"value": dist.sum(float(e2e_steps)) / t_e2e, "unit": "loads/s",
                 "h2d_bytes_per_step": int(bases.nbytes + lind.nbytes), "d2h_bytes_per_step": out_bytes,
                 "call": "linac_gb300.cuda_load_matrix (host arrays)"},
-        "roofline": {"bound": "hbm", "kernel": "load_matrix_kernel", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "load_pairs_kernel" if p < 2**31 else "load_matrix_kernel",
+                     "achieved": achieved,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                     "traffic": None, "bytes_per_launch": alg_bytes,
-                     "peak_source": f"{peaks['source']} copy bandwidth"},
+                     "traffic": LOADER_TRAFFIC_PER_BYTE * alg_bytes if p < 2**31 else None,
+                     "bytes_per_launch": alg_bytes,
+                     "peak_source": f"{peaks['source']} copy bandwidth",
+                     "note": "at degree 8 the pair-product lookups (shared memory) and lazy Shoup multiplies "
+                             "bound the kernel, not HBM; traffic from one ncu capture of this launch"},
         "cpu_baseline": cpu, "clocks": clk.summary(),
     }
 

@@ -7,26 +7,31 @@
 // 138-196).  Here the whole panel (K = 128 pivots) is applied in one
 // contraction, exactly, on the BF16 tensor cores:
 //
-//  * every residue x (centred to (-p/2, p/2)) is split into four balanced
-//    base-256 digits x = sum_i d_i 256^i, d_i in [-128, 128]; integers of that
-//    size are exact in BF16;
-//  * a digit product is at most 2^14 in magnitude, and the four products that
+//  * every residue x (centred to (-p/2, p/2]) is split into four balanced
+//    base-256 digits x = sum_i d_i 256^i, |d_i| <= 128; integers of that size
+//    are exact in BF16;
+//  * a digit product is at most 2^14 in magnitude, and the products that
 //    share a weight 256^s (s = i + j) summed over K = 128 stay below 2^23, so
 //    every FP32 accumulation in TMEM is an exact integer;
-//  * the epilogue converts the seven group sums D_s to integers, forms
-//    sum_s D_s * (256^s mod p) in 64-bit, reduces it mod p (Barrett) and adds
-//    it to the old residue.
+//  * the epilogue converts the seven group sums D_s to integers (x + 1.5 2^23
+//    where |x| <= 2^22, F2I otherwise), forms sum_s D_s (256^s mod p) in
+//    64-bit, reduces it mod p (one Montgomery step for 2^30 <= p < 2^31, the
+//    weights carrying the factor 2^32; Barrett otherwise) and adds it to the
+//    old residue.
 //
 // Layout: the four E digit planes are K-major (row = matrix row, 128 digits),
-// the B digits are stacked per 64-column output tile as 4 x 64 K-major rows, so
-// one UMMA (M = 128, N = 256, K = 16) multiplies digit plane i of E with all
-// four digit planes of B and lands in TMEM columns [64 i, 64 i + 256): the
+// the B digits are stacked per 32-column output tile as 4 x 32 K-major rows, so
+// one UMMA (M = 128, N = 128, K = 16) multiplies digit plane i of E with all
+// four digit planes of B and lands in TMEM columns [32 i, 32 i + 128): the
 // column block s = i + j accumulates exactly the weight-256^s products.
 //
-// Kernel: one CTA per 128-row block and up to 8 consecutive 64-column tiles;
-// warp 0 issues TMA loads (E digits once, B digits double-buffered), warp 1
-// issues the UMMAs and owns the TMEM allocation, warps 2-5 drain TMEM, combine,
-// write C and re-zero their TMEM lanes for the next tile.
+// Kernel (tc_kernels.cuh): one CTA per 128-row block and a run of consecutive
+// 32-column tiles (chosen to fill whole waves of the GPU); warp 0 issues the
+// TMA loads (E digits once, B digits through a 4-stage ring), warp 1 issues
+// the UMMAs and owns the TMEM allocation (two accumulators of 7 x 32 columns,
+// so the epilogue of one tile overlaps the UMMAs of the next), warps 2-9
+// (two per TMEM lane quarter, 16 columns each) drain TMEM, re-zero it,
+// combine and write C.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>

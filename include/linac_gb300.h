@@ -104,6 +104,8 @@ int lnc_event_create(void** event);
 int lnc_event_destroy(void* event);
 int lnc_event_record(void* event, void* stream);
 int lnc_event_elapsed_ms(void* start, void* stop, float* ms);
+/* Later work on `stream` waits for `event` (recorded on another stream). */
+int lnc_stream_wait_event(void* stream, void* event);
 /* Read (and clear) the device-side error word; returns the status it held
  * (LNC_OK when none): LNC_ERR_TIMEOUT from a bounded wait that ran out,
  * LNC_ERR_INVALID from lnc_load_matrix_device given an index past the end of

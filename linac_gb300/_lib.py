@@ -90,6 +90,7 @@ _SIGNATURES = {
     "lnc_event_destroy": ([_vp], _int),
     "lnc_event_record": ([_vp, _vp], _int),
     "lnc_event_elapsed_ms": ([_vp, _vp, _vp], _int),
+    "lnc_stream_wait_event": ([_vp, _vp], _int),
     "lnc_device_status": ([], _int),
     "lnc_kernel_timing_enable": ([_int], _int),
     "lnc_kernel_timing_reset": ([], _int),
@@ -277,6 +278,10 @@ class Event:
 
     def record(self, stream=None):
         check(lib().lnc_event_record(self.handle, stream.handle if isinstance(stream, Stream) else stream))
+
+    def wait_on(self, stream):
+        """Make later work on `stream` wait for this event."""
+        check(lib().lnc_stream_wait_event(stream.handle if isinstance(stream, Stream) else stream, self.handle))
 
     def elapsed_ms(self, end: "Event") -> float:
         ms = ctypes.c_float()

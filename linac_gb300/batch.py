@@ -159,6 +159,87 @@ class BatchPlan:
             pass
 
 
+class PipelinedBatch:
+    """A batch cut into consecutive chunks of about equal work, one BatchPlan
+    (one CUDA graph) each, so that the host-to-device copy of chunk k + 1, the
+    graph of chunk k and the copy back of chunk k - 1 overlap: the copies run
+    on two copy streams, every graph on its own stream behind an event of its
+    input copy, and a graph's tail (few large matrices left) overlaps the next
+    chunk's graph."""
+
+    def __init__(self, shapes, primes, chunks: int = 4, tiles_per_cta: int = 0, cand_rows: int = 0):
+        _bind()
+        shapes = [(int(m), int(n)) for m, n in shapes]
+        primes = [int(p) for p in primes]
+        if len(shapes) != len(primes) or not shapes:
+            raise ValueError("need one prime per matrix and at least one matrix")
+        work = np.array([m * n * min(m, n) for m, n in shapes], dtype=np.float64)
+        cum = np.cumsum(work)
+        chunks = max(1, min(int(chunks), len(shapes)))
+        cuts = [0] + [int(np.searchsorted(cum, cum[-1] * k / chunks)) + 1 for k in range(1, chunks)] + [len(shapes)]
+        cuts = sorted(set(min(max(c, 0), len(shapes)) for c in cuts))
+        self.bounds = [(a, b) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
+        self.plans = [BatchPlan(shapes[a:b], primes[a:b], tiles_per_cta, cand_rows, stream=_lib.Stream())
+                      for a, b in self.bounds]
+        self.s_in, self.s_out = _lib.Stream(), _lib.Stream()
+        self.ev_in = [_lib.Event() for _ in self.plans]
+        self.ev_done = [_lib.Event() for _ in self.plans]
+        self.redone = 0
+
+    @property
+    def device_bytes(self) -> int:
+        return sum(p.device_bytes for p in self.plans)
+
+    def pinned_buffers(self):
+        """One pinned host buffer per chunk (layout of BatchPlan.pack)."""
+        return [_lib.PinnedArray((p.total_bytes,), np.uint8).array for p in self.plans]
+
+    def pack(self, matrices, bufs=None):
+        bufs = bufs if bufs is not None else self.pinned_buffers()
+        for (a, b), p, buf in zip(self.bounds, self.plans, bufs):
+            p.pack(matrices[a:b], out=buf)
+        return bufs
+
+    def run(self, host_in, host_out) -> int:
+        """Copy every chunk in, reduce it and copy it back, overlapped;
+        returns the number of matrices redone by the exhaustive path."""
+        L = _lib.lib()
+        for k, p in enumerate(self.plans):
+            _lib.check(L.lnc_memcpy_h2d(p.d_in.ptr, host_in[k].ctypes.data, p.total_bytes, self.s_in.handle))
+            self.ev_in[k].record(self.s_in)
+            self.ev_in[k].wait_on(p.stream)
+            p.run()
+            self.ev_done[k].record(p.stream)
+            self.ev_done[k].wait_on(self.s_out)
+            _lib.check(L.lnc_memcpy_d2h(host_out[k].ctypes.data, p.d_out.ptr, p.total_bytes, self.s_out.handle))
+        self.s_out.synchronize()
+        self.redone = 0
+        for k, p in enumerate(self.plans):
+            r = p.finish()
+            if r:  # matrices redone after their chunk was copied back: copy the chunk again
+                p.download_packed(host_out[k])
+            self.redone += r
+        return self.redone
+
+    def unpack(self, host_out):
+        res = []
+        for p, buf in zip(self.plans, host_out):
+            res.extend(p.unpack(buf))
+        return res
+
+    def pivots_and_ranks(self):
+        pivs, ranks = [], []
+        for p in self.plans:
+            pv, rk = p.pivots_and_ranks()
+            pivs.extend(pv)
+            ranks.extend(int(x) for x in rk)
+        return pivs, np.array(ranks, dtype=np.int64)
+
+    def close(self):
+        for p in self.plans:
+            p.close()
+
+
 def _residues_u64(A: np.ndarray, q: int) -> np.ndarray:
     """Entries of A reduced to [0, q) as uint64 (integer or object arrays)."""
     if A.dtype == object:
@@ -172,6 +253,10 @@ def _residues_u64(A: np.ndarray, q: int) -> np.ndarray:
         return np.mod(a, np.int64(q)).astype(np.uint64)
     # q > |a|: a mod q is a, or a + q for a negative a (two's complement wraps to it)
     return a.view(np.uint64) + (a < 0).astype(np.uint64) * np.uint64(q)
+
+
+# batches of at least this many input bytes are cut into overlapped chunks
+PIPELINE_BYTES = 256 << 20
 
 
 def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True):
@@ -199,6 +284,18 @@ def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True)
         return res
     shapes = [A.shape for A in mats]
     tpc, cand = autotune(shapes, primes) if tune else (0, 0)
+    if sum(4 * m * n for m, n in shapes) >= PIPELINE_BYTES and len(shapes) >= 8:
+        pb = PipelinedBatch(shapes, primes, 4, tpc, cand)
+        try:
+            outs = pb.pinned_buffers()
+            pb.run(pb.pack(mats), outs)
+            res = [R.copy() for R in pb.unpack(outs)]
+            if return_pivots:
+                pivs, _ = pb.pivots_and_ranks()
+                return res, [[int(x) for x in p] for p in pivs]
+            return res
+        finally:
+            pb.close()
     plan = BatchPlan(shapes, primes, tpc, cand)
     try:
         host = plan.pack(mats)

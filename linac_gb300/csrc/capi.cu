@@ -405,6 +405,10 @@ int lnc_event_create(void** e) {
 }
 int lnc_event_destroy(void* e) { LNC_CUDA(cudaEventDestroy((cudaEvent_t)e)); return LNC_OK; }
 int lnc_event_record(void* e, void* s) { LNC_CUDA(cudaEventRecord((cudaEvent_t)e, (cudaStream_t)s)); return LNC_OK; }
+int lnc_stream_wait_event(void* s, void* e) {
+    LNC_CUDA(cudaStreamWaitEvent((cudaStream_t)s, (cudaEvent_t)e, 0));
+    return LNC_OK;
+}
 int lnc_event_elapsed_ms(void* a, void* b, float* ms) {
     LNC_CUDA(cudaEventSynchronize((cudaEvent_t)b));
     LNC_CUDA(cudaEventElapsedTime(ms, (cudaEvent_t)a, (cudaEvent_t)b));

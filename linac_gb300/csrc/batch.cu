@@ -472,13 +472,10 @@ static int plan_create(const lnc_batch_matrix* mats, int64_t count, int tpc, int
         for (int t = 0; t < 5; ++t) x *= 2u - p * x;
         d.pinv = 0u - x;
         d.r2 = (uint32_t)((((unsigned __int128)1) << 64) % p);
-        d.redc = ((p & 1u) && p >= (1u << 30) && p < (1u << 31)) ? 1 : 0;
-        uint64_t w = d.redc ? (((uint64_t)1 << 32) % p) : (1 % p);
-        for (int g = 0; g < tc::GROUPS; ++g) {
-            d.w[g] = (w > p / 2) ? (int32_t)((int64_t)w - (int64_t)p) : (int32_t)w;
-            w = (w * 256) % p;
-        }
-        d.off = ((((uint64_t)1 << 59) + p - 1) / p) * p;
+        const tc::LimbConstants lc = tc::limb_constants(p);
+        d.redc = lc.redc;
+        for (int g = 0; g < tc::GROUPS; ++g) d.w[g] = lc.w[g];
+        d.off = lc.off;
     }
     // ---- per-step active lists and work lists (static: they depend on the shapes only)
     std::vector<int> order(count);

@@ -61,6 +61,36 @@ struct LimbJob {
     const double* cscale;
 };
 
+// Epilogue constants of the limb contraction for a prime p < 2^32 (host side).
+// The epilogue forms v = off + sum_s D_s w_s (w_s = 256^s R mod p, centred,
+// so |w_s| <= p / 2) in 64-bit arithmetic and reduces it mod p.
+//  * odd p < 2^31: R = 2^32 mod p and one Montgomery step (v 2^-32 mod p),
+//    valid for 0 <= v < 2^32 p.  The digit-group sums (paired or not) weigh
+//    at most 1.52 * 2^30 in magnitude in total, so |sum| <= 0.76 * 2^30 p and
+//    off = 2^30 p keeps v inside [0.24, 1.76] * 2^30 p;
+//  * p = 2 and 2^31 <= p < 2^32: R = 1 and Barrett; |sum| < 2^61.6 and off is
+//    the first multiple of p at or above 2^62.
+struct LimbConstants {
+    int redc;
+    int32_t w[GROUPS];
+    uint64_t off;
+    uint32_t pinv;  // -p^-1 mod 2^32
+};
+static inline LimbConstants limb_constants(uint32_t p) {
+    LimbConstants c;
+    c.redc = ((p & 1u) && p < (1u << 31)) ? 1 : 0;
+    uint64_t w = c.redc ? (((uint64_t)1 << 32) % p) : (1 % p);
+    for (int g = 0; g < GROUPS; ++g) {
+        c.w[g] = (w > p / 2) ? (int32_t)((int64_t)w - (int64_t)p) : (int32_t)w;
+        w = (w * 256) % p;
+    }
+    c.off = c.redc ? ((uint64_t)p << 30) : (((((uint64_t)1 << 62) + p - 1) / p) * p);
+    uint32_t x = p;
+    for (int i = 0; i < 5; ++i) x *= 2u - p * x;
+    c.pinv = 0u - x;
+    return c;
+}
+
 struct TcParams {
     uint32_t* C;            // trailing block base: A + j1
     int64_t ldc;
@@ -70,8 +100,8 @@ struct TcParams {
     int n_tiles;            // 64-column tiles covering N
     const int32_t* panel_k;
     FieldU32 f;
-    int32_t w[GROUPS];      // 256^s mod p, centred
-    uint64_t off;           // multiple of p >= 2^59 (makes the 64-bit sum non-negative)
+    int32_t w[GROUPS];      // 256^s R mod p, centred (limb_constants)
+    uint64_t off;           // multiple of p keeping the 64-bit epilogue sum in range (limb_constants)
     int overwrite;          // 1: C <- E * B (C is not read), 0: C <- C + E * B
     uint32_t pinv;          // -p^-1 mod 2^32 (Montgomery reduction of the epilogue sum)
     int redc;
@@ -186,8 +216,9 @@ __device__ __forceinline__ void flag_error(const LimbJob& P, volatile int* cta_e
     atomicExch(P.status, LNC_ERR_TIMEOUT);
 }
 
-// v mod p for the epilogue sum v < 2^60: Montgomery (v 2^-32; the weights
-// already carry the factor 2^32) when 2^30 <= p < 2^31, else Barrett.
+// v mod p for the epilogue sum: Montgomery (v 2^-32, valid for 0 <= v < 2^32
+// p; the weights already carry the factor 2^32) for odd p < 2^31, else
+// Barrett (any 64-bit v).
 template <bool REDC>
 __device__ __forceinline__ uint32_t reduce_sum(const FieldU32& f, uint32_t pinv, uint64_t v) {
     if (REDC) {
@@ -199,9 +230,9 @@ __device__ __forceinline__ uint32_t reduce_sum(const FieldU32& f, uint32_t pinv,
     }
 }
 
-// One CTA of the limb GEMM (see the file comment).  REDC (J.redc): 2^30 <= p
-// < 2^31, the weights carry an extra factor 2^32 and the 64-bit digit sum is
-// reduced by one Montgomery step; otherwise Barrett.
+// One CTA of the limb GEMM (see the file comment).  REDC (J.redc): odd p <
+// 2^31, the weights carry an extra factor 2^32 and the 64-bit digit sum is
+// reduced by one Montgomery step; otherwise Barrett (limb_constants).
 // Exact value of the digit-product sum of one output element (float
 // epilogue): the seven group sums are integers below 2^24 in magnitude, so
 // hi (groups 3..6) and lo (groups 0..2) are exact in int64 and the result
@@ -356,6 +387,12 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
             wsum += w[g];
         }
         const uint64_t bias = P.off - (uint64_t)((int64_t)MAGIC_I * wsum);
+        // integer fast path: groups (0, 1) and (5, 6) are paired before weighting, z = y_g + 256 y_{g+1}
+        // (w_{g+1} = 256 w_g mod p), from one shift-add of their conversion bits; the first group of a
+        // pair is converted negated (sign bit set), which leaves z + KPAIR in int32 range
+        constexpr int32_t KPAIR = 0x0B400000;  // (257 * MAGIC_I + 2^31) mod 2^32
+        const uint64_t bias2 = P.off - (uint64_t)((int64_t)KPAIR * ((int64_t)w[0] + w[5])) -
+                               (uint64_t)((int64_t)MAGIC_I * ((int64_t)w[2] + w[3] + w[4]));
         if constexpr (FLOAT) {
             // output element (row, col): F64 -> Cd[row * ldc + col];  C128 -> part (row & 1) of
             // Cd[(row >> 1) * ldc + col] (complex elements, viewed as pairs of doubles)
@@ -478,14 +515,23 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
                     for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
                 const bool fast = mx <= 4194304.0f;
                 if (__all_sync(0xffffffffu, fast)) {
+                    // |y_0|, |y_6| <= 2^21 and |y_1|, |y_5| <= 2^22 for any digits: |z_01| <= 2^30 + 2^21,
+                    // |z_56| <= 2^29 + 2^22; five 64-bit multiply-adds instead of seven
 #pragma unroll
                     for (int c = 0; c < 16; ++c) {
-                        uint64_t v = (uint64_t)bias;
+                        const uint32_t b0n = __float_as_uint(__fadd_rn(-__uint_as_float(d[0][c]), -MAGIC_F));
+                        const uint32_t b1 = __float_as_uint(__fadd_rn(__uint_as_float(d[1][c]), MAGIC_F));
+                        const uint32_t b5n = __float_as_uint(__fadd_rn(-__uint_as_float(d[5][c]), -MAGIC_F));
+                        const uint32_t b6 = __float_as_uint(__fadd_rn(__uint_as_float(d[6][c]), MAGIC_F));
+                        const int32_t z01 = (int32_t)((b1 << 8) + b0n);  // z_01 + KPAIR
+                        const int32_t z56 = (int32_t)((b6 << 8) + b5n);  // z_56 + KPAIR
+                        uint64_t v = bias2 + (uint64_t)((int64_t)z01 * (int64_t)w[0]);
 #pragma unroll
-                        for (int g = 0; g < GROUPS; ++g) {
+                        for (int g = 2; g <= 4; ++g) {
                             const int32_t y = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F));
                             v += (uint64_t)((int64_t)y * (int64_t)w[g]);
                         }
+                        v += (uint64_t)((int64_t)z56 * (int64_t)w[5]);
                         old[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
                     }
                 } else {

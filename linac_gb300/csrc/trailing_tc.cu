@@ -15,9 +15,9 @@
 //    every FP32 accumulation in TMEM is an exact integer;
 //  * the epilogue converts the seven group sums D_s to integers (x + 1.5 2^23
 //    where |x| <= 2^22, F2I otherwise), forms sum_s D_s (256^s mod p) in
-//    64-bit, reduces it mod p (one Montgomery step for 2^30 <= p < 2^31, the
-//    weights carrying the factor 2^32; Barrett otherwise) and adds it to the
-//    old residue.
+//    64-bit (groups (0, 1) and (5, 6) paired first by a shift-add), reduces
+//    it mod p (one Montgomery step for odd p < 2^31, the weights carrying the
+//    factor 2^32; Barrett otherwise) and adds it to the old residue.
 //
 // Layout: the four E digit planes are K-major (row = matrix row, 128 digits),
 // the B digits are stacked per 32-column output tile as 4 x 32 K-major rows, so
@@ -192,19 +192,12 @@ int tc_limb_gemm(const FieldU32& f, uint32_t* C, int64_t ldc, int64_t m, int64_t
     P.n_tiles = n_tiles;
     P.panel_k = k_ptr;
     P.f = f;
-    const bool redc = (p & 1u) && p >= (1u << 30) && p < (1u << 31);
-    uint64_t w = redc ? (((uint64_t)1 << 32) % p) : (1 % p);  // 2^32 folded in for the Montgomery step
-    for (int sgrp = 0; sgrp < GROUPS; ++sgrp) {
-        P.w[sgrp] = (w > p / 2) ? (int32_t)((int64_t)w - (int64_t)p) : (int32_t)w;
-        w = (w * 256) % p;
-    }
-    P.off = ((((uint64_t)1 << 59) + p - 1) / p) * p;
+    const LimbConstants lc = limb_constants(p);
+    const bool redc = lc.redc != 0;
+    for (int sgrp = 0; sgrp < GROUPS; ++sgrp) P.w[sgrp] = lc.w[sgrp];
+    P.off = lc.off;
     P.overwrite = overwrite ? 1 : 0;
-    {
-        uint32_t x = p;
-        for (int i = 0; i < 5; ++i) x *= 2u - p * x;
-        P.pinv = 0u - x;
-    }
+    P.pinv = lc.pinv;
     P.err = err;
     P.status = status;
     P.redc = redc ? 1 : 0;

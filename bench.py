@@ -350,11 +350,25 @@ def run_ours(args, dist: Dist):
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
     cuda_row_reduce(host_in, p, out=host_out)  # warm
     dist.barrier()
+    call_ms = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        tc = time.perf_counter()
         R, pv = cuda_row_reduce(host_in, p, out=host_out, return_pivots=True)
+        call_ms.append(1e3 * (time.perf_counter() - tc))
     t_e2e = dist.max(time.perf_counter() - t0)
     e2e_value = dist.sum(float(e2e_steps)) / t_e2e
+    # the host link on its own: the same bytes each way between the pinned buffers and HBM
+    ev_c = [_lib.Event() for _ in range(3)]
+    ev_c[0].record(stream.handle)
+    d_work.upload(host_in, stream.handle)
+    ev_c[1].record(stream.handle)
+    d_out.download(host_out, stream.handle)
+    ev_c[2].record(stream.handle)
+    stream.synchronize()
+    link = {"h2d_gbs": nbytes / (ev_c[0].elapsed_ms(ev_c[1]) * 1e6),
+            "d2h_gbs": nbytes / (ev_c[1].elapsed_ms(ev_c[2]) * 1e6),
+            "calls_ms": call_ms}
 
     # ---- roofline of the dominant kernel class ----
     peaks = measured_peaks()
@@ -429,7 +443,7 @@ def run_ours(args, dist: Dist):
                        "min": float(min(lat)), "max": float(max(lat))},
         "bit_exact": ident_ok,
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes + 8 * (kmax + 1), "call": "linac_gb300.cuda_row_reduce"},
+                "d2h_bytes_per_step": nbytes + 8 * (kmax + 1), "call": "linac_gb300.cuda_row_reduce", **link},
         "gpu_launches": launches,
         "kernel_ms": {k: {"launches": v[0], "total_ms": v[1], "work": kt_work[k]} for k, v in kt.items()},
         "roofline": roof,
@@ -1456,7 +1470,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="batched workloads: skip the autotuner")
     ap.add_argument("--plain-sample", type=int, default=64)
-    ap.add_argument("--float-workers", type=int, default=8, help="float batch: host worker threads")
+    ap.add_argument("--float-workers", type=int, default=16, help="float batch: host worker threads")
     ap.add_argument("--serve-requests", type=int, default=0, help="served workload: requests per step")
     ap.add_argument("--serve-inflight", type=int, default=16, help="served workload: requests in flight")
     ap.add_argument("--serve-rate", type=float, default=float("inf"),

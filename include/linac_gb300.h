@@ -204,7 +204,7 @@ int64_t lnc_batch_plan_bytes(void* plan);
 int lnc_batch_plan_destroy(void* plan);
 /* LNC_U32: create + run + finish + destroy.  LNC_U64 (a prime per matrix, up
  * to 2^64 - 59; no captured plan): every matrix through the single-matrix
- * 64-bit path, on 8 worker threads with their own streams, after the work
+ * 64-bit path, on 16 worker threads with their own streams, after the work
  * already queued on `stream`; synchronous.  Inputs are not modified. */
 int lnc_rref_batch_device(int dtype, const lnc_batch_matrix* mats, int64_t count, void* stream, int flags);
 
@@ -219,7 +219,7 @@ typedef struct lnc_mixed_result {
  * RREF of `count` float64 / complex128 matrices of any sizes (LNC_F64 or
  * LNC_C128; `p` of each descriptor is ignored), `tol` the head threshold
  * (<= 0: 1e-9), flags as for lnc_rref_device (LNC_FLAG_MIXED for the
- * mixed-precision path).  `workers` host threads (<= 0: 8), each with its own
+ * mixed-precision path).  `workers` host threads (<= 0: 16), each with its own
  * stream, take the matrices in order and solve them concurrently; inputs are
  * not modified.  reports (optional, count entries) receives each solve's
  * mixed-precision report.  Synchronous.

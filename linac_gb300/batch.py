@@ -374,7 +374,7 @@ class ConcurrentBatch:
         _lib.check(_lib.lib().lnc_memcpy_h2d(self.d_in.ptr, packed.ctypes.data, self.total_bytes, stream))
         _lib.check(_lib.lib().lnc_stream_synchronize(stream))
 
-    def run(self, mixed: bool = True, workers: int = 8, tol: float = 1e-9):
+    def run(self, mixed: bool = True, workers: int = 16, tol: float = 1e-9):
         if self.modp:
             _lib.check(_lib.lib().lnc_rref_batch_device(self.code, ctypes.addressof(self._descs), len(self.shapes),
                                                         None, 0), "lnc_rref_batch_device")
@@ -417,7 +417,7 @@ class FloatBatch(ConcurrentBatch):
         super().__init__(shapes, dtype)
 
 
-def rref_float_batch(matrices, mixed: bool = True, workers: int = 8, return_pivots: bool = False,
+def rref_float_batch(matrices, mixed: bool = True, workers: int = 16, return_pivots: bool = False,
                      return_reports: bool = False, tol: float = 1e-9):
     """RREF of every float64 / complex128 matrix of the list (linac's float
     semantics: rows pre-scaled by their largest |a|, partial pivoting,

@@ -144,7 +144,7 @@ int concurrent_batch(int dtype, const lnc_batch_matrix* mats, int64_t count, dou
     S.mats = mats;
     S.reports = reports;
     S.count = count;
-    const int W = (int)std::max<int64_t>(1, std::min<int64_t>(workers > 0 ? workers : 8, count));
+    const int W = (int)std::max<int64_t>(1, std::min<int64_t>(workers > 0 ? workers : 16, count));
     std::vector<std::thread> pool;
     pool.reserve((size_t)W);
     for (int w = 0; w < W; ++w) pool.emplace_back(worker, &S);

@@ -485,6 +485,12 @@ int plan_rref(int64_t m, int64_t n, RrefPlan* plan) {
     if (rc) return rc;
     if (!di.coop) { set_error("device does not support cooperative launches"); return LNC_ERR_UNSUPPORTED; }
     int G = (int)std::min<int64_t>(di.sms, m);
+    if constexpr (F::kDtype >= 3) {
+        // float panels: at least 32 rows per CTA.  Fewer CTAs make the per-column grid barrier
+        // cheaper and leave SMs to the panels of concurrent solves (a batch of 64 float systems,
+        // n ~ U[256, 4096], 16 workers: 67 -> 80 solves/s); a 5000-row panel is unchanged
+        G = (int)std::max<int64_t>(1, std::min<int64_t>(G, (m + 31) / 32));
+    }
     int R = (int)((m + G - 1) / G);
     G = (int)((m + R - 1) / R);
     const size_t budget = (size_t)di.smem_optin - 8 * 1024;  // static smem headroom

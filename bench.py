@@ -394,7 +394,9 @@ def run_ours(args, dist: Dist):
             peak = peaks["bf16_tflops_sustained"]
             roof = {"bound": "tensor", "kernel": "tc64::limb64_gemm_kernel" if u64 else "tc::limb_gemm_kernel",
                     "achieved": achieved, "peak": peak,
-                    "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic_per_launch(args.workload, "limb_gemm"),
+                    "unit": "TFLOP/s", "frac": achieved / peak,
+                    "traffic": (traffic_per_launch(args.workload, "limb_gemm") if u64 else
+                                LIMB_U32_TRAFFIC_PER_C_BYTE * 8.0 * work / 128.0 / max(1, kt["trailing"][0])),
                     "peak_source": f"{peaks['source']} bf16 sustained (kernel timed inside a long solve)",
                     "work_unit": ("field multiply-adds m*N*64 per launch, x 2*8*8 bf16 flops" if u64
                                   else "field multiply-adds m*N*128 per launch, x 2*4*4 bf16 flops"),
@@ -547,10 +549,16 @@ def trailing_bytes(m: int, n: int, b: int) -> float:
 # the launches of one ncu capture of the same workload (dram__bytes_read.sum +
 # dram__bytes_write.sum, one pass of the whole-workload launch list)
 PROFILED_TRAFFIC = {
-    ("rref_u32_20000", "limb_gemm"): 322.0e6,   # look-ahead schedule: near, far and E = G X launches
     ("rref_u64_8000", "trailing_simt"): 465.4e6,
     ("rref_u64_8000", "limb_gemm"): 97.4e6,     # look-ahead schedule
 }
+
+# 32-bit limb contraction: DRAM bytes per byte of C read and written, from one
+# `--set full` capture of a single 8192 x 8192 x 128 launch (limb_gemm_8192):
+# 501.8 MB of DRAM traffic for 536.9 MB of C (the operand digits add 17 MB;
+# the last writes were still in L2 when the kernel ended).  A launch's
+# traffic is this ratio times its 8 m N bytes of C.
+LIMB_U32_TRAFFIC_PER_C_BYTE = 501.8e6 / 536.9e6
 
 
 # loader: DRAM bytes per algorithmic byte of one load_pairs_kernel launch
@@ -1350,7 +1358,8 @@ def run_serve(args, dist: Dist):
     lat_reqs = make(max(2 * per_step, 32))
     run_phase(srv, lat_reqs, 0.7 * value / dist.world)
     st_lat = srv.stats()
-    # ---- plain path on two requests of every degree; served results must match it bit for bit
+    # ---- plain path on up to four requests of every degree (median time); served results must match
+    # it bit for bit
     plain_t, exact = {}, True
     by_d = {}
     for r in (x for b in reqs for x in b):
@@ -1358,7 +1367,7 @@ def run_serve(args, dist: Dist):
     cuda_row_reduce(cuda_load_matrix(*reqs[0][0][2:4], field_characteristic=reqs[0][0][1]), reqs[0][0][1])
     for d, rs in sorted(by_d.items()):
         ts = []
-        for (dd, p, bases, lind) in rs[:2]:
+        for (dd, p, bases, lind) in rs[:4]:
             t0 = time.perf_counter()
             A = cuda_load_matrix(bases, lind, (bases.shape[0], lind.shape[0]), field_characteristic=p)
             R_plain, piv_plain = cuda_row_reduce(A, field_characteristic=p, return_pivots=True)
@@ -1367,7 +1376,7 @@ def run_serve(args, dist: Dist):
             R, piv, rank = t.result(copy=False)
             exact = exact and bool(np.array_equal(R, R_plain)) and piv == piv_plain
             t.release()
-        plain_t[d] = float(np.mean(ts))
+        plain_t[d] = float(np.median(ts))
     plain_s = sum(plain_t[r[0]] for b in reqs for r in b)
     plain_value = per_step * args.steps / plain_s
     srv.close()

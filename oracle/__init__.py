@@ -47,6 +47,9 @@ def _load():
     global _lib
     with _lock:
         if _lib is None:
+            # OpenMP threads sleep as soon as a parallel region ends instead of spinning, so that
+            # an oracle check does not take host cores from the timed GPU work that follows it
+            os.environ.setdefault("OMP_WAIT_POLICY", "passive")
             build()
             lib = ctypes.CDLL(_LIB_PATH)
             i64, u64, dbl, vp, cint = (ctypes.c_int64, ctypes.c_uint64, ctypes.c_double,

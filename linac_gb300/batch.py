@@ -159,6 +159,19 @@ class BatchPlan:
             pass
 
 
+def chunk_bounds(shapes, chunks: int):
+    """Cut a list of matrix shapes into at most `chunks` consecutive, non-empty
+    ranges [a, b) of about equal work (m n min(m, n) each)."""
+    work = np.array([m * n * min(m, n) for m, n in shapes], dtype=np.float64)
+    if len(work) == 0:
+        return []
+    cum = np.cumsum(work)
+    chunks = max(1, min(int(chunks), len(shapes)))
+    cuts = [0] + [int(np.searchsorted(cum, cum[-1] * k / chunks)) + 1 for k in range(1, chunks)] + [len(shapes)]
+    cuts = sorted(set(min(max(c, 0), len(shapes)) for c in cuts))
+    return [(a, b) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
+
+
 class PipelinedBatch:
     """A batch cut into consecutive chunks of about equal work, one BatchPlan
     (one CUDA graph) each, so that the host-to-device copy of chunk k + 1, the
@@ -173,12 +186,7 @@ class PipelinedBatch:
         primes = [int(p) for p in primes]
         if len(shapes) != len(primes) or not shapes:
             raise ValueError("need one prime per matrix and at least one matrix")
-        work = np.array([m * n * min(m, n) for m, n in shapes], dtype=np.float64)
-        cum = np.cumsum(work)
-        chunks = max(1, min(int(chunks), len(shapes)))
-        cuts = [0] + [int(np.searchsorted(cum, cum[-1] * k / chunks)) + 1 for k in range(1, chunks)] + [len(shapes)]
-        cuts = sorted(set(min(max(c, 0), len(shapes)) for c in cuts))
-        self.bounds = [(a, b) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
+        self.bounds = chunk_bounds(shapes, chunks)
         self.plans = [BatchPlan(shapes[a:b], primes[a:b], tiles_per_cta, cand_rows, stream=_lib.Stream())
                       for a, b in self.bounds]
         self.s_in, self.s_out = _lib.Stream(), _lib.Stream()

@@ -272,3 +272,24 @@ def test_u64_candidate_panel_misses_are_redone(flags):
     R_ref, piv_ref, _ = oracle.rref_modp(A, p)
     assert np.array_equal(out, R_ref)
     assert piv == piv_ref
+
+
+def test_large_host_outputs_fresh_strided_and_in_place():
+    """Pageable host outputs of 64 MB and more are mapped by host threads while
+    the GPU solves: the default fresh output, a strided output (the columns
+    between its rows stay untouched) and an in-place call (the input is read
+    before anything is written) all hold the exact result."""
+    p = 2**31 - 1
+    m = 4200  # 4200 x 4200 uint32: 70.6 MB; full rank with overwhelming probability, so the RREF is I
+    rng = np.random.default_rng(11)
+    A = rng.integers(0, p, size=(m, m), dtype=np.uint64).astype(np.uint32)
+    eye = np.eye(m, dtype=np.uint32)
+    R, piv = cuda_row_reduce(A, p, return_pivots=True)
+    assert piv == list(range(m)) and np.array_equal(R, eye)
+    big = np.full((m, m + 5), 7, dtype=np.uint32)
+    out = big[:, :m]
+    cuda_row_reduce(A, p, out=out)
+    assert np.array_equal(out, eye) and np.all(big[:, m:] == 7)
+    B = A.copy()
+    cuda_row_reduce(B, p, out=B)
+    assert np.array_equal(B, eye)

@@ -280,7 +280,23 @@ def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True)
     mats = [np.asarray(A) for A in matrices]
     if isinstance(primes, (int, np.integer)):
         primes = [int(primes)] * len(mats)
-    if any(int(q) > 2**32 - 1 for q in primes):
+    if len(primes) != len(mats):
+        raise ValueError("one prime per matrix")
+    if any(A.ndim != 2 for A in mats):
+        raise ValueError("rref_batch expects 2-D matrices")
+    wide = any(int(q) > 2**32 - 1 for q in primes)
+    empty = [i for i, A in enumerate(mats) if A.size == 0]
+    if empty:  # an empty matrix is its own RREF, without pivots
+        full = [i for i, A in enumerate(mats) if A.size != 0]
+        dt = np.uint64 if wide else np.uint32
+        res = [np.zeros(A.shape, dtype=dt) for A in mats]
+        pivs = [[] for _ in mats]
+        if full:
+            sub = rref_batch([mats[i] for i in full], [primes[i] for i in full], return_pivots=True, tune=tune)
+            for i, R, pv in zip(full, *sub):
+                res[i], pivs[i] = R, pv
+        return (res, pivs) if return_pivots else res
+    if wide:
         cb = ConcurrentBatch([A.shape for A in mats], np.uint64, primes)
         packed = cb.pack([_residues_u64(A, int(q)) for A, q in zip(mats, primes)])
         cb.upload(packed)

@@ -50,6 +50,8 @@ template <class Arith, class W, int PW, int CL>
 static int launch_cand_cluster(const CandArgs& a, double elt, cudaStream_t s) {
     auto kern = cand_cluster_kernel<Arith, W, PW, CL>;
     const size_t smem = cand_cluster_smem<W, PW, CL>(a.smax);
+    int rc = allow_dynamic_smem((const void*)kern, smem);
+    if (rc) return rc;
     ScopedKernelTimer kt(KC_PANEL, s, 2.0 * a.smax * a.bw * elt);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(CL, 1, 1);

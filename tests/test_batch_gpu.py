@@ -149,3 +149,17 @@ def test_pipelined_batch_chunks_match_oracle():
         assert redone >= 1
     finally:
         pb.close()
+
+
+@pytest.mark.parametrize("wide", [False, True])
+def test_batch_with_empty_matrices(wide):
+    """Empty matrices in a batch come back as empty RREFs without pivots; the
+    others are reduced as usual (32- and 64-bit residues)."""
+    p = 2**61 - 1 if wide else 2**31 - 1
+    rng = np.random.default_rng(8)
+    A = rng.integers(0, p, size=(50, 60), dtype=np.uint64)
+    mats = [np.zeros((0, 7), dtype=np.uint64), A, np.zeros((5, 0), dtype=np.uint64)]
+    res, pivs = rref_batch(mats, [p, p, p], return_pivots=True, tune=False)
+    assert res[0].shape == (0, 7) and res[2].shape == (5, 0) and pivs[0] == [] and pivs[2] == []
+    R_ref, piv_ref, _ = oracle.rref_modp(A, p)
+    assert np.array_equal(res[1].astype(np.uint64), R_ref) and pivs[1] == piv_ref

@@ -177,8 +177,8 @@ class PipelinedBatch:
     (one CUDA graph) each, so that the host-to-device copy of chunk k + 1, the
     graph of chunk k and the copy back of chunk k - 1 overlap: the copies run
     on two copy streams, every graph on its own stream behind an event of its
-    input copy, and a graph's tail (few large matrices left) overlaps the next
-    chunk's graph."""
+    input copy, and the graphs of consecutive chunks overlap one another (a
+    graph's last steps hold few large matrices)."""
 
     def __init__(self, shapes, primes, chunks: int = 4, tiles_per_cta: int = 0, cand_rows: int = 0):
         _bind()
@@ -267,6 +267,12 @@ def _residues_u64(A: np.ndarray, q: int) -> np.ndarray:
 PIPELINE_BYTES = 256 << 20
 
 
+def pipeline_chunks(count: int) -> int:
+    """Chunks of a pipelined batch: about 128 matrices each, 2 to 32 (the 4096-matrix benchmark batch
+    end to end: 7.7k solves/s with 4 chunks, 8.6k with 16, 9.5k with 32; 10.4k on the device)."""
+    return max(2, min(32, count // 128))
+
+
 def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True):
     """RREF of every matrix of the list over F_{primes[i]}.
 
@@ -309,7 +315,7 @@ def rref_batch(matrices, primes, return_pivots: bool = False, tune: bool = True)
     shapes = [A.shape for A in mats]
     tpc, cand = autotune(shapes, primes) if tune else (0, 0)
     if sum(4 * m * n for m, n in shapes) >= PIPELINE_BYTES and len(shapes) >= 8:
-        pb = PipelinedBatch(shapes, primes, 4, tpc, cand)
+        pb = PipelinedBatch(shapes, primes, pipeline_chunks(len(shapes)), tpc, cand)
         try:
             outs = pb.pinned_buffers()
             pb.run(pb.pack(mats), outs)

@@ -811,6 +811,17 @@ def run_batch(args, dist: Dist):
         pb.run(e2e_in, e2e_out)
     t_e2e = dist.max(time.perf_counter() - t0)
     e2e_value = dist.sum(float(e2e_runs * len(specs))) / t_e2e
+    # the same chunks with their inputs resident: graphs only, overlapping on their streams
+    t0 = time.perf_counter()
+    for _ in range(e2e_runs):
+        pb.run_device()
+    chunked_value = dist.sum(float(e2e_runs * len(specs))) / dist.max(time.perf_counter() - t0)
+    # ... and every chunk graph as a child of one graph, one launch per run
+    pb.run_graph()
+    t0 = time.perf_counter()
+    for _ in range(e2e_runs):
+        pb.run_graph()
+    grouped_value = dist.sum(float(e2e_runs * len(specs))) / dist.max(time.perf_counter() - t0)
     e2e_outs = pb.unpack(e2e_out)
     for i in small:
         ok = ok and bool(np.array_equal(e2e_outs[i], outs[i]))
@@ -856,6 +867,10 @@ def run_batch(args, dist: Dist):
         "plain": {"value": plain_value, "unit": "solves/s", "sample": int(len(sample)),
                   "call": "linac_gb300.cuda_row_reduce per matrix (host arrays)",
                   "note": "sample rate scaled to the batch's mean m*n*min(m,n)"},
+        "chunked": {"value": chunked_value, "unit": "solves/s", "chunks": len(pb.plans),
+                    "note": "the e2e path's chunk graphs on resident inputs (host wall time, no copies)"},
+        "grouped": {"value": grouped_value, "unit": "solves/s", "chunks": len(pb.plans),
+                    "note": "the chunk graphs as child graphs of one graph, one launch (host wall time)"},
         "batched_vs_plain": value / plain_value,
         "batched_e2e_vs_plain": e2e_value / plain_value,
         "gpu_launches": launches,

@@ -201,6 +201,15 @@ int lnc_batch_plan_run(void* plan, void* stream);
 int lnc_batch_plan_finish(void* plan, void* stream, int64_t* n_redo);
 /* Device bytes held by the plan (admission accounting). */
 int64_t lnc_batch_plan_bytes(void* plan);
+/* One CUDA graph over `count` plans (a batch cut into chunks): each plan's
+ * graph is a child graph, with no dependency between plans, so one launch
+ * (lnc_batch_group_run, asynchronous) reduces every chunk and the GPU
+ * overlaps them.  The plans must outlive the group; lnc_batch_plan_finish of
+ * each plan completes a run.  No counterpart in the reference (see
+ * lnc_batch_plan_create). */
+int lnc_batch_group_create(void* const* plans, int64_t count, void** group);
+int lnc_batch_group_run(void* group, void* stream);
+int lnc_batch_group_destroy(void* group);
 int lnc_batch_plan_destroy(void* plan);
 /* LNC_U32: create + run + finish + destroy.  LNC_U64 (a prime per matrix, up
  * to 2^64 - 59; no captured plan): every matrix through the single-matrix

@@ -47,6 +47,9 @@ def _bind():
     _lib.bind("lnc_batch_plan_destroy", [vp])
     _lib.bind("lnc_rref_batch_device", [ci, vp, i64, vp, ci])
     _lib.bind("lnc_rref_float_batch", [ci, vp, i64, ctypes.c_double, ci, ci, vp])
+    _lib.bind("lnc_batch_group_create", [vp, i64, vp])
+    _lib.bind("lnc_batch_group_run", [vp, vp])
+    _lib.bind("lnc_batch_group_destroy", [vp])
     _bound = True
 
 
@@ -190,6 +193,8 @@ class PipelinedBatch:
         self.plans = [BatchPlan(shapes[a:b], primes[a:b], tiles_per_cta, cand_rows, stream=_lib.Stream())
                       for a, b in self.bounds]
         self.s_in, self.s_out = _lib.Stream(), _lib.Stream()
+        self._group = None
+        self.s_group = None
         self.ev_in = [_lib.Event() for _ in self.plans]
         self.ev_done = [_lib.Event() for _ in self.plans]
         self.redone = 0
@@ -229,6 +234,38 @@ class PipelinedBatch:
             self.redone += r
         return self.redone
 
+    def run_device(self) -> int:
+        """Reduce the chunks already on the device (their graphs overlap on
+        their own streams); returns the number of matrices redone."""
+        for p in self.plans:
+            p.run()
+        self.redone = sum(p.finish() for p in self.plans)
+        return self.redone
+
+    def launch_graph(self):
+        """One launch, on ``self.s_group``, of a graph whose child graphs are
+        every chunk's graph (no dependency between chunks); asynchronous, and
+        ordered after the work already queued on every chunk's stream."""
+        if self._group is None:
+            h = ctypes.c_void_p()
+            arr = (ctypes.c_void_p * len(self.plans))(*[p.handle for p in self.plans])
+            _lib.check(_lib.lib().lnc_batch_group_create(arr, len(self.plans), ctypes.byref(h)),
+                       "lnc_batch_group_create")
+            self._group = h.value
+            self.s_group = _lib.Stream()
+        for ev, p in zip(self.ev_in, self.plans):
+            ev.record(p.stream)
+            ev.wait_on(self.s_group)
+        _lib.check(_lib.lib().lnc_batch_group_run(self._group, self.s_group.handle), "lnc_batch_group_run")
+
+    def run_graph(self) -> int:
+        """Reduce the chunks already on the device with one graph launch
+        (launch_graph); returns the number of matrices redone."""
+        self.launch_graph()
+        self.s_group.synchronize()
+        self.redone = sum(p.finish() for p in self.plans)
+        return self.redone
+
     def unpack(self, host_out):
         res = []
         for p, buf in zip(self.plans, host_out):
@@ -244,6 +281,9 @@ class PipelinedBatch:
         return pivs, np.array(ranks, dtype=np.int64)
 
     def close(self):
+        if self._group is not None:
+            _lib.lib().lnc_batch_group_destroy(self._group)
+            self._group = None
         for p in self.plans:
             p.close()
 

@@ -616,6 +616,67 @@ int batch_finish(BatchPlan* P, cudaStream_t s, int64_t* n_redo) {
     return LNC_OK;
 }
 
+// One graph over several plans: every plan's graph becomes a child graph of
+// the group, behind a memset node that clears that plan's error words, with
+// no dependency between plans, so one launch runs all of them and the GPU
+// overlaps their steps (one plan's last steps, which hold few large
+// matrices, run beside the other plans' work).
+struct BatchGroup {
+    std::vector<BatchPlan*> plans;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches_per_run = 0;
+};
+
+int batch_group_create(BatchPlan* const* plans, int64_t count, BatchGroup** out) {
+    if (count <= 0) { set_error("empty plan group"); return LNC_ERR_INVALID; }
+    BatchGroup* G = new BatchGroup();
+    int rc = LNC_OK;
+    cudaError_t e = cudaGraphCreate(&G->graph, 0);
+    for (int64_t i = 0; e == cudaSuccess && i < count; ++i) {
+        BatchPlan* P = plans[i];
+        if (!P || !P->graph) { rc = LNC_ERR_INVALID; set_error("plan %lld of the group is not a batch plan", (long long)i); break; }
+        cudaMemsetParams mp = {};
+        mp.dst = P->d_words;
+        mp.value = 0;
+        mp.elementSize = 4;
+        mp.width = 2;
+        mp.height = 1;
+        mp.pitch = 0;
+        cudaGraphNode_t ms = nullptr, child = nullptr;
+        e = cudaGraphAddMemsetNode(&ms, G->graph, nullptr, 0, &mp);
+        if (e == cudaSuccess) e = cudaGraphAddChildGraphNode(&child, G->graph, &ms, 1, P->graph);
+        G->plans.push_back(P);
+        G->launches_per_run += P->launches_per_run;
+    }
+    if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&G->exec, G->graph, 0);
+    if (!rc && e != cudaSuccess) rc = cuda_status(e, "plan group graph");
+    if (rc) {
+        if (G->exec) cudaGraphExecDestroy(G->exec);
+        if (G->graph) cudaGraphDestroy(G->graph);
+        delete G;
+        return rc;
+    }
+    *out = G;
+    return LNC_OK;
+}
+
+int batch_group_run(BatchGroup* G, cudaStream_t s) {
+    {
+        ScopedKernelTimer kt(KC_BATCH, s);
+        LNC_CUDA(cudaGraphLaunch(G->exec, s));
+    }
+    for (int64_t i = 0; i < G->launches_per_run; ++i) count_launch();
+    return LNC_OK;
+}
+
+void batch_group_destroy(BatchGroup* G) {
+    if (!G) return;
+    if (G->exec) cudaGraphExecDestroy(G->exec);
+    if (G->graph) cudaGraphDestroy(G->graph);
+    delete G;
+}
+
 void batch_destroy(BatchPlan* P) {
     if (!P) return;
     if (P->exec) cudaGraphExecDestroy(P->exec);

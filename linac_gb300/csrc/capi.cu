@@ -307,6 +307,10 @@ int batch_run(BatchPlan* P, cudaStream_t s);
 int batch_finish(BatchPlan* P, cudaStream_t s, int64_t* n_redo);
 void batch_destroy(BatchPlan* P);
 size_t batch_plan_bytes(BatchPlan* P);
+struct BatchGroup;
+int batch_group_create(BatchPlan* const* plans, int64_t count, BatchGroup** out);
+int batch_group_run(BatchGroup* G, cudaStream_t s);
+void batch_group_destroy(BatchGroup* G);
 
 }  // namespace lnc
 
@@ -626,6 +630,24 @@ int64_t lnc_batch_plan_bytes(void* plan) { return (int64_t)batch_plan_bytes((Bat
 
 int lnc_batch_plan_destroy(void* plan) {
     batch_destroy((BatchPlan*)plan);
+    return LNC_OK;
+}
+
+int lnc_batch_group_create(void* const* plans, int64_t count, void** group) {
+    if (!plans || !group) { set_error("null argument"); return LNC_ERR_INVALID; }
+    BatchGroup* G = nullptr;
+    int rc = batch_group_create((BatchPlan* const*)plans, count, &G);
+    *group = rc ? nullptr : (void*)G;
+    return rc;
+}
+
+int lnc_batch_group_run(void* group, void* stream) {
+    if (!group) { set_error("null plan group"); return LNC_ERR_INVALID; }
+    return batch_group_run((BatchGroup*)group, (cudaStream_t)stream);
+}
+
+int lnc_batch_group_destroy(void* group) {
+    batch_group_destroy((BatchGroup*)group);
     return LNC_OK;
 }
 

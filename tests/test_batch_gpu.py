@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle
-from linac_gb300 import workloads
+from linac_gb300 import _lib, workloads
 from linac_gb300.batch import BatchPlan, rref_batch
 
 pytestmark = pytest.mark.gpu
@@ -147,6 +147,19 @@ def test_pipelined_batch_chunks_match_oracle():
                 assert np.array_equal(R.astype(np.uint64), R_ref)
                 assert [int(x) for x in pv] == piv_ref
         assert redone >= 1
+        # the same chunks through one launch of the grouped graph, twice
+        for _ in range(2):
+            for p, buf in zip(pb.plans, ins):
+                p.upload_packed(buf)
+                _lib.check(_lib.lib().lnc_memset(p.d_out.ptr, 0xFF, p.total_bytes, p.stream.handle))
+            assert pb.run_graph() >= 1
+            outs = [p.download_packed(np.zeros_like(buf)) for p, buf in zip(pb.plans, ins)]
+            res = pb.unpack(outs)
+            pivs, _ = pb.pivots_and_ranks()
+            for M, q, R, pv in zip(mats, primes, res, pivs):
+                R_ref, piv_ref, _ = oracle.rref_modp(M, q)
+                assert np.array_equal(R.astype(np.uint64), R_ref)
+                assert [int(x) for x in pv] == piv_ref
     finally:
         pb.close()
 

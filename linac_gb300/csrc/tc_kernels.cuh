@@ -380,13 +380,8 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
             ptx::mbar_arrive(&acc_empty[1]);
         }
         int32_t w[GROUPS];  // weights in registers (P.w may alias nothing, but the compiler cannot tell)
-        int64_t wsum = 0;   // sum of the weights: removes the magic offset in one step
 #pragma unroll
-        for (int g = 0; g < GROUPS; ++g) {
-            w[g] = FLOAT ? 0 : P.w[g];
-            wsum += w[g];
-        }
-        const uint64_t bias = P.off - (uint64_t)((int64_t)MAGIC_I * wsum);
+        for (int g = 0; g < GROUPS; ++g) w[g] = FLOAT ? 0 : P.w[g];
         // integer fast path: groups (0, 1) and (5, 6) are paired before weighting, z = y_g + 256 y_{g+1}
         // (w_{g+1} = 256 w_g mod p), from one shift-add of their conversion bits; the first group of a
         // pair is converted negated (sign bit set), which leaves z + KPAIR in int32 range

@@ -66,10 +66,10 @@ struct LimbJob {
 // so |w_s| <= p / 2) in 64-bit arithmetic and reduces it mod p.
 //  * odd p < 2^31: R = 2^32 mod p and one Montgomery step (v 2^-32 mod p),
 //    valid for 0 <= v < 2^32 p.  The digit-group sums (paired or not) weigh
-//    at most 1.52 * 2^30 in magnitude in total, so |sum| <= 0.76 * 2^30 p and
-//    off = 2^30 p keeps v inside [0.24, 1.76] * 2^30 p;
-//  * p = 2 and 2^31 <= p < 2^32: R = 1 and Barrett; |sum| < 2^61.6 and off is
-//    the first multiple of p at or above 2^62.
+//    at most 2.52 * 2^30 in magnitude in total, so |sum| <= 1.26 * 2^30 p and
+//    off = 1.5 * 2^30 p keeps v inside [0.24, 2.76] * 2^30 p;
+//  * p = 2 and 2^31 <= p < 2^32: R = 1 and Barrett; |sum| < 1.26 * 2^61 and
+//    off is the first multiple of p at or above 2^62.
 struct LimbConstants {
     int redc;
     int32_t w[GROUPS];
@@ -84,7 +84,7 @@ static inline LimbConstants limb_constants(uint32_t p) {
         c.w[g] = (w > p / 2) ? (int32_t)((int64_t)w - (int64_t)p) : (int32_t)w;
         w = (w * 256) % p;
     }
-    c.off = c.redc ? ((uint64_t)p << 30) : (((((uint64_t)1 << 62) + p - 1) / p) * p);
+    c.off = c.redc ? (((uint64_t)p * 3) << 29) : (((((uint64_t)1 << 62) + p - 1) / p) * p);
     uint32_t x = p;
     for (int i = 0; i < 5; ++i) x *= 2u - p * x;
     c.pinv = 0u - x;
@@ -218,15 +218,26 @@ __device__ __forceinline__ void flag_error(const LimbJob& P, volatile int* cta_e
 
 // v mod p for the epilogue sum: Montgomery (v 2^-32, valid for 0 <= v < 2^32
 // p; the weights already carry the factor 2^32) for odd p < 2^31, else
-// Barrett (any 64-bit v).
+// Barrett (any 64-bit v).  Montgomery: with m = v pinv mod 2^32, v + m p is a
+// multiple of 2^32 below 2^33 p <= 2^64, and (v + m p) / 2^32 < 2p.
 template <bool REDC>
 __device__ __forceinline__ uint32_t reduce_sum(const FieldU32& f, uint32_t pinv, uint64_t v) {
     if (REDC) {
-        const uint32_t lo = (uint32_t)v;
-        const uint32_t u = (uint32_t)(v >> 32) + __umulhi(lo * pinv, f.p) + (lo != 0u ? 1u : 0u);  // < 2p
+        const uint32_t m = (uint32_t)v * pinv;
+        const uint32_t u = (uint32_t)(((uint64_t)m * f.p + v) >> 32);  // < 2p
         return min(u, u - f.p);
     } else {
         return f.reduce64(v);
+    }
+}
+// old + r mod p for residues old, r < p (p < 2^31 when REDC: no 64-bit sum)
+template <bool REDC>
+__device__ __forceinline__ uint32_t add_residue(const FieldU32& f, uint32_t old, uint32_t r) {
+    if (REDC) {
+        const uint32_t s = old + r;
+        return min(s, s - f.p);
+    } else {
+        return f.add(old, r);
     }
 }
 
@@ -382,12 +393,13 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
         int32_t w[GROUPS];  // weights in registers (P.w may alias nothing, but the compiler cannot tell)
 #pragma unroll
         for (int g = 0; g < GROUPS; ++g) w[g] = FLOAT ? 0 : P.w[g];
-        // integer fast path: groups (0, 1) and (5, 6) are paired before weighting, z = y_g + 256 y_{g+1}
-        // (w_{g+1} = 256 w_g mod p), from one shift-add of their conversion bits; the first group of a
-        // pair is converted negated (sign bit set), which leaves z + KPAIR in int32 range
+        // integer fast path: groups (0, 1), (2, 3) and (5, 6) are paired before weighting,
+        // z = y_g + 256 y_{g+1} (w_{g+1} = 256 w_g mod p), from one shift-add of their conversion bits;
+        // the first group of a pair is converted negated (sign bit set), which leaves z + KPAIR in
+        // int32 range
         constexpr int32_t KPAIR = 0x0B400000;  // (257 * MAGIC_I + 2^31) mod 2^32
-        const uint64_t bias2 = P.off - (uint64_t)((int64_t)KPAIR * ((int64_t)w[0] + w[5])) -
-                               (uint64_t)((int64_t)MAGIC_I * ((int64_t)w[2] + w[3] + w[4]));
+        const uint64_t bias3 = P.off - (uint64_t)((int64_t)KPAIR * ((int64_t)w[0] + w[2] + w[5])) -
+                               (uint64_t)((int64_t)MAGIC_I * (int64_t)w[4]);
         if constexpr (FLOAT) {
             // output element (row, col): F64 -> Cd[row * ldc + col];  C128 -> part (row & 1) of
             // Cd[(row >> 1) * ldc + col] (complex elements, viewed as pairs of doubles)
@@ -500,34 +512,36 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
                 if (lane == 0) ptx::mbar_arrive(&acc_empty[buf]);
                 if (t + 1 < ntiles) load_old(t + 1, oldn);
                 // exact conversion: for |x| <= 2^22, x + 1.5 * 2^23 is exact and its bit pattern minus
-                // 0x4B400000 is x (full-rate FADD instead of the quarter-rate F2I).  Groups 0, 1, 5, 6 hold
-                // at most two digit products per step and stay within 2^22 for any input; groups 2-4 are
-                // checked.  The weighted sum is formed modulo 2^64; its true value lies in [0, 2^60].
+                // 0x4B400000 is x (full-rate FADD instead of the quarter-rate F2I).  Digits 0-2 lie in
+                // [-128, 127] and the top digit in [-64, 64] for p < 2^31 ([-128, 128] otherwise), so
+                // groups 0, 1, 5, 6 stay within 2^22 for any input, group 4 too for p < 2^31; groups
+                // 2, 3 (and 4 for p >= 2^31) are checked.  The weighted sum is formed modulo 2^64.
                 float mx = 0.f;
 #pragma unroll
-                for (int g = 2; g <= 4; ++g)
+                for (int g = 2; g <= (REDC ? 3 : 4); ++g)
 #pragma unroll
                     for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
                 const bool fast = mx <= 4194304.0f;
                 if (__all_sync(0xffffffffu, fast)) {
-                    // |y_0|, |y_6| <= 2^21 and |y_1|, |y_5| <= 2^22 for any digits: |z_01| <= 2^30 + 2^21,
-                    // |z_56| <= 2^29 + 2^22; five 64-bit multiply-adds instead of seven
+                    // |y_0|, |y_6| <= 2^21, |y_1|, |y_5| <= 2^22, |y_2|, |y_3|, |y_4| <= 2^22 here:
+                    // |z_01|, |z_23| <= 2^30 + 2^22, |z_56| <= 2^29 + 2^22; four 64-bit multiply-adds
 #pragma unroll
                     for (int c = 0; c < 16; ++c) {
                         const uint32_t b0n = __float_as_uint(__fadd_rn(-__uint_as_float(d[0][c]), -MAGIC_F));
                         const uint32_t b1 = __float_as_uint(__fadd_rn(__uint_as_float(d[1][c]), MAGIC_F));
+                        const uint32_t b2n = __float_as_uint(__fadd_rn(-__uint_as_float(d[2][c]), -MAGIC_F));
+                        const uint32_t b3 = __float_as_uint(__fadd_rn(__uint_as_float(d[3][c]), MAGIC_F));
+                        const int32_t b4 = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[4][c]), MAGIC_F));
                         const uint32_t b5n = __float_as_uint(__fadd_rn(-__uint_as_float(d[5][c]), -MAGIC_F));
                         const uint32_t b6 = __float_as_uint(__fadd_rn(__uint_as_float(d[6][c]), MAGIC_F));
                         const int32_t z01 = (int32_t)((b1 << 8) + b0n);  // z_01 + KPAIR
+                        const int32_t z23 = (int32_t)((b3 << 8) + b2n);  // z_23 + KPAIR
                         const int32_t z56 = (int32_t)((b6 << 8) + b5n);  // z_56 + KPAIR
-                        uint64_t v = bias2 + (uint64_t)((int64_t)z01 * (int64_t)w[0]);
-#pragma unroll
-                        for (int g = 2; g <= 4; ++g) {
-                            const int32_t y = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F));
-                            v += (uint64_t)((int64_t)y * (int64_t)w[g]);
-                        }
+                        uint64_t v = bias3 + (uint64_t)((int64_t)z01 * (int64_t)w[0]);
+                        v += (uint64_t)((int64_t)z23 * (int64_t)w[2]);
+                        v += (uint64_t)((int64_t)b4 * (int64_t)w[4]);  // y_4 + MAGIC_I
                         v += (uint64_t)((int64_t)z56 * (int64_t)w[5]);
-                        old[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
+                        old[c] = add_residue<REDC>(f, old[c], reduce_sum<REDC>(f, P.pinv, v));
                     }
                 } else {
 #pragma unroll
@@ -536,7 +550,7 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
 #pragma unroll
                         for (int g = 0; g < GROUPS; ++g)
                             v += (uint64_t)((int64_t)__float2int_rn(__uint_as_float(d[g][c])) * (int64_t)w[g]);
-                        old[c] = f.add(old[c], reduce_sum<REDC>(f, P.pinv, v));
+                        old[c] = add_residue<REDC>(f, old[c], reduce_sum<REDC>(f, P.pinv, v));
                     }
                 }
                 if (vec) {

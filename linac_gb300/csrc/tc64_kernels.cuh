@@ -221,56 +221,76 @@ static __global__ void __launch_bounds__(THREADS, 1)
 
     if (warp == 0) {
         // ------------------------------------------------------------ producer
-        if (lane == 0) {
+        // warp-wide loops, elected lanes issue (see elect_one in tc_ptx.cuh)
+        const bool leader = ptx::elect_one();
+        if (leader) {
             ptx::prefetch_tmap(&tmA);
             ptx::prefetch_tmap(&tmB);
             ptx::mbar_expect_tx(a_full, LIMBS * A_TILE_BYTES);
             for (int i = 0; i < LIMBS; ++i)
                 ptx::tma_load_2d(sA + i * A_TILE_BYTES, &tmA, a_full, 0, i * P.m_pad + rb * BM);
-            int issued_round[STAGES];
-            for (int st = 0; st < STAGES; ++st) issued_round[st] = -1;
-            for (int t = 0; t < ntiles && !s_err; ++t) {
-                const int st = t % STAGES, round = t / STAGES;
-                if (!ptx::mbar_wait(&b_empty[st], (round & 1) ^ 1, &s_err)) { flag_error64(P, &s_err); break; }
+        }
+        int issued_round[STAGES];
+        for (int st = 0; st < STAGES; ++st) issued_round[st] = -1;
+        for (int t = 0; t < ntiles; ++t) {
+            if (__any_sync(0xffffffffu, s_err != 0)) break;
+            const int st = t % STAGES, round = t / STAGES;
+            if (!__all_sync(0xffffffffu, ptx::mbar_wait(&b_empty[st], (round & 1) ^ 1, &s_err))) {
+                if (leader) flag_error64(P, &s_err);
+                break;
+            }
+            if (leader) {
                 ptx::mbar_expect_tx(&b_full[st], B_TILE_BYTES);
                 ptx::tma_load_2d(sB + st * B_TILE_BYTES, &tmB, &b_full[st], 0, (t0 + t) * B_ROWS);
-                issued_round[st] = round;
             }
+            issued_round[st] = round;
+            __syncwarp();
+        }
+        if (leader) {
             const long long lim = kSpinLimitCycles / 4;
             ptx::mbar_wait_nocancel(a_full, 0, lim);
             for (int st = 0; st < STAGES; ++st)
                 if (issued_round[st] >= 0) ptx::mbar_wait_nocancel(&b_full[st], issued_round[st] & 1, lim);
         }
+        __syncwarp();
     } else if (warp == 1) {
         // ------------------------------------------------------------ MMA issuer
-        if (lane == 0) {
-            constexpr uint32_t idesc = ptx::umma_idesc_bf16(BM, B_ROWS);
-            const uint64_t adesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sA));  // K steps move the address field
-            const uint64_t bdesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sB));
-            bool ok = ptx::mbar_wait(a_full, 0, &s_err);
-            if (!ok) flag_error64(P, &s_err);
-            const int ksteps = (k + 15) / 16;  // K steps beyond k are all zero (and skipped)
-            for (int t = 0; t < ntiles && ok; ++t) {
-                const int buf = t & 1;
-                const int st = t % STAGES, round = t / STAGES;
-                if (!ptx::mbar_wait(&acc_empty[buf], (t >> 1) & 1, &s_err)) { flag_error64(P, &s_err); break; }
-                if (!ptx::mbar_wait(&b_full[st], round & 1, &s_err)) { flag_error64(P, &s_err); break; }
-                ptx::tc_fence_after();
-                const uint32_t dbase = tmem + ACC_STRIDE * buf;
-                for (int ks = 0; ks < ksteps; ++ks) {
-                    const uint64_t bdesc = bdesc0 + (uint64_t)((st * B_TILE_BYTES + ks * 32) >> 4);
+        const bool leader = ptx::elect_one();
+        constexpr uint32_t idesc = ptx::umma_idesc_bf16(BM, B_ROWS);
+        const uint64_t adesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sA));  // K steps move the address field
+        const uint64_t bdesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sB));
+        bool ok = __all_sync(0xffffffffu, ptx::mbar_wait(a_full, 0, &s_err));
+        if (!ok && leader) flag_error64(P, &s_err);
+        const int ksteps = (k + 15) / 16;  // K steps beyond k are all zero (and skipped)
+        for (int t = 0; t < ntiles && ok; ++t) {
+            const int buf = t & 1;
+            const int st = t % STAGES, round = t / STAGES;
+            if (!__all_sync(0xffffffffu, ptx::mbar_wait(&acc_empty[buf], (t >> 1) & 1, &s_err)) ||
+                !__all_sync(0xffffffffu, ptx::mbar_wait(&b_full[st], round & 1, &s_err))) {
+                if (leader) flag_error64(P, &s_err);
+                break;
+            }
+            ptx::tc_fence_after();
+            const uint32_t dbase = tmem + ACC_STRIDE * buf;
+            for (int ks = 0; ks < ksteps; ++ks) {
+                const uint64_t bdesc = bdesc0 + (uint64_t)((st * B_TILE_BYTES + ks * 32) >> 4);
 #pragma unroll
-                    for (int i = 0; i < LIMBS; ++i) {
-                        const uint64_t adesc = adesc0 + (uint64_t)((i * A_TILE_BYTES + ks * 32) >> 4);
-                        ptx::umma_bf16(dbase + (uint32_t)(BN * i), adesc, bdesc, idesc, 1u);
-                    }
+                for (int i = 0; i < LIMBS; ++i) {
+                    const uint64_t adesc = adesc0 + (uint64_t)((i * A_TILE_BYTES + ks * 32) >> 4);
+                    if (leader) ptx::umma_bf16(dbase + (uint32_t)(BN * i), adesc, bdesc, idesc, 1u);
                 }
+            }
+            if (leader) {
                 ptx::umma_commit(&b_empty[st]);
                 ptx::umma_commit(&acc_full[buf]);
             }
+            __syncwarp();
+        }
+        if (leader) {
             ptx::umma_commit(drain);
             ptx::mbar_wait_nocancel(drain, 0, kSpinLimitCycles / 4);
         }
+        __syncwarp();
     } else {
         // ------------------------------------------------------------ epilogue
         const int ew = warp - 2;

@@ -254,9 +254,17 @@ __device__ __forceinline__ double fx_digit_value(const int32_t (&y)[GROUPS]) {
     return fma((double)hi, 16777216.0, (double)lo);
 }
 
+// mbarrier wait of the producer / MMA warp: warp-uniform by a vote when the whole warp runs the loop
+template <bool WIDE>
+__device__ __forceinline__ bool issuer_wait(uint64_t* bar, uint32_t parity, volatile int* cta_err) {
+    const bool got = ptx::mbar_wait(bar, parity, cta_err);
+    return WIDE ? __all_sync(0xffffffffu, got) : got;
+}
+
 template <int EPI>
 __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tmA, const CUtensorMap* tmB) {
     constexpr bool REDC = EPI == EPI_REDC;
+    constexpr bool WIDE = EPI != EPI_BARRETT;  // producer / MMA loops run by the whole warp
     constexpr bool FLOAT = EPI == EPI_F64 || EPI == EPI_C128;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte alignment for the 128-byte swizzle atoms
@@ -304,9 +312,11 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
     ptx::tc_fence_after();
     const uint32_t tmem = *s_tmem;
 
-    if (warp == 0) {
+    if (warp == 0 && (WIDE || lane == 0)) {
         // ------------------------------------------------------------ producer
-        if (lane == 0) {
+        // warp-wide loop (WIDE), the elected lane issues the copies (as for the MMA issuer)
+        const bool leader = WIDE ? ptx::elect_one() : true;
+        if (leader) {
             ptx::prefetch_tmap(tmA);
             ptx::prefetch_tmap(tmB);
             ptx::mbar_expect_tx(a_full, LIMBS * nkc * A_TILE_BYTES);
@@ -314,63 +324,89 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
                 for (int kc = 0; kc < nkc; ++kc)
                     ptx::tma_load_2d(sA + (i * NKC + kc) * A_TILE_BYTES, tmA, a_full, kc * KC,
                                      P.a_row0 + i * P.a_plane + rb * BM);
-            int it = 0;
-            int issued_round[STAGES];
-            for (int st = 0; st < STAGES; ++st) issued_round[st] = -1;
-            for (int t = 0; t < ntiles && !s_err; ++t) {
-                for (int kc = 0; kc < nkc; ++kc, ++it) {
-                    const int st = it % STAGES, round = it / STAGES;
-                    if (!ptx::mbar_wait(&b_empty[st], (round & 1) ^ 1, &s_err)) { flag_error(P, &s_err); break; }
+        }
+        int it = 0;
+        int issued_round[STAGES];
+        for (int st = 0; st < STAGES; ++st) issued_round[st] = -1;
+        bool go = true;
+        for (int t = 0; t < ntiles && go; ++t) {
+            if (WIDE ? __any_sync(0xffffffffu, s_err != 0) : (s_err != 0)) break;
+            for (int kc = 0; kc < nkc; ++kc, ++it) {
+                const int st = it % STAGES, round = it / STAGES;
+                if (!issuer_wait<WIDE>(&b_empty[st], (round & 1) ^ 1, &s_err)) {
+                    if (leader) flag_error(P, &s_err);
+                    go = false;
+                    break;
+                }
+                if (leader) {
                     ptx::mbar_expect_tx(&b_full[st], B_TILE_BYTES);
                     ptx::tma_load_2d(sB + st * B_TILE_BYTES, tmB, &b_full[st], kc * KC, P.b_row0 + (t0 + t) * B_ROWS);
-                    issued_round[st] = round;
                 }
+                issued_round[st] = round;
+                if (WIDE) __syncwarp();
             }
-            // never leave with copies in flight: wait (bounded) for every load issued
+        }
+        // never leave with copies in flight: wait (bounded) for every load issued
+        if (leader) {
             const long long lim = kSpinLimitCycles / 4;
             ptx::mbar_wait_nocancel(a_full, 0, lim);
             for (int st = 0; st < STAGES; ++st)
                 if (issued_round[st] >= 0) ptx::mbar_wait_nocancel(&b_full[st], issued_round[st] & 1, lim);
         }
-    } else if (warp == 1) {
+        if (WIDE) __syncwarp();
+    } else if (warp == 1 && (WIDE || lane == 0)) {
         // ------------------------------------------------------------ MMA issuer
-        if (lane == 0) {
-            constexpr uint32_t idesc = ptx::umma_idesc_bf16(BM, B_ROWS);
-            // descriptors of the ring / plane bases; a K step or a stage moves only the start-address
-            // field (address / 16, 14 bits: shared-memory offsets never carry out of it)
-            const uint64_t adesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sA));
-            const uint64_t bdesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sB));
-            bool ok = ptx::mbar_wait(a_full, 0, &s_err);
-            if (!ok) flag_error(P, &s_err);
-            int it = 0;
-            for (int t = 0; t < ntiles && ok; ++t) {
-                const int buf = t & 1;
-                if (!ptx::mbar_wait(&acc_empty[buf], (t >> 1) & 1, &s_err)) { flag_error(P, &s_err); break; }
-                ptx::tc_fence_after();
-                const uint32_t dbase = tmem + ACC_STRIDE * buf;
-                for (int kc = 0; kc < nkc && ok; ++kc, ++it) {
-                    const int st = it % STAGES, round = it / STAGES;
-                    if (!ptx::mbar_wait(&b_full[st], round & 1, &s_err)) { flag_error(P, &s_err); ok = false; break; }
-                    ptx::tc_fence_after();
-#pragma unroll
-                    for (int ks = 0; ks < KC / 16; ++ks) {
-                        const uint64_t bdesc = bdesc0 + (uint64_t)((st * B_TILE_BYTES + ks * 32) >> 4);
-#pragma unroll
-                        for (int i = 0; i < LIMBS; ++i) {
-                            const uint64_t adesc =
-                                adesc0 + (uint64_t)(((i * NKC + kc) * A_TILE_BYTES + ks * 32) >> 4);
-                            ptx::umma_bf16(dbase + (uint32_t)(BN * i), adesc, bdesc, idesc, 1u);
-                        }
-                    }
-                    ptx::umma_commit(&b_empty[st]);  // stage reusable once these UMMAs finish
-                }
-                if (ok) ptx::umma_commit(&acc_full[buf]);
+        // WIDE: the whole warp runs the loop, so the descriptor arithmetic stays warp-uniform; the
+        // elected lane issues the UMMAs and their commits, and every wait is decided by a warp vote
+        // (without it, integer work on this SM sub-partition slows the UMMA stream).  The Barrett
+        // epilogue, whose heavier combine bounds the kernel, runs faster with lane 0 alone.
+        const bool leader = WIDE ? ptx::elect_one() : true;
+        constexpr uint32_t idesc = ptx::umma_idesc_bf16(BM, B_ROWS);
+        // descriptors of the ring / plane bases; a K step or a stage moves only the start-address
+        // field (address / 16, 14 bits: shared-memory offsets never carry out of it)
+        const uint64_t adesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sA));
+        const uint64_t bdesc0 = ptx::umma_desc_sw128(ptx::smem_u32(sB));
+        bool ok = issuer_wait<WIDE>(a_full, 0, &s_err);
+        if (!ok && leader) flag_error(P, &s_err);
+        int it = 0;
+        for (int t = 0; t < ntiles && ok; ++t) {
+            const int buf = t & 1;
+            if (!issuer_wait<WIDE>(&acc_empty[buf], (t >> 1) & 1, &s_err)) {
+                if (leader) flag_error(P, &s_err);
+                break;
             }
-            // all issued UMMAs complete before the TMEM is released
+            ptx::tc_fence_after();
+            const uint32_t dbase = tmem + ACC_STRIDE * buf;
+            for (int kc = 0; kc < nkc && ok; ++kc, ++it) {
+                const int st = it % STAGES, round = it / STAGES;
+                if (!issuer_wait<WIDE>(&b_full[st], round & 1, &s_err)) {
+                    if (leader) flag_error(P, &s_err);
+                    ok = false;
+                    break;
+                }
+                ptx::tc_fence_after();
+#pragma unroll
+                for (int ks = 0; ks < KC / 16; ++ks) {
+                    const uint64_t bdesc = bdesc0 + (uint64_t)((st * B_TILE_BYTES + ks * 32) >> 4);
+#pragma unroll
+                    for (int i = 0; i < LIMBS; ++i) {
+                        const uint64_t adesc = adesc0 + (uint64_t)(((i * NKC + kc) * A_TILE_BYTES + ks * 32) >> 4);
+                        if (leader) ptx::umma_bf16(dbase + (uint32_t)(BN * i), adesc, bdesc, idesc, 1u);
+                    }
+                }
+                if (leader) ptx::umma_commit(&b_empty[st]);  // stage reusable once these UMMAs finish
+                if (WIDE) __syncwarp();
+            }
+            if (ok && leader) ptx::umma_commit(&acc_full[buf]);
+            if (WIDE) __syncwarp();
+        }
+        // all issued UMMAs complete before the TMEM is released
+        if (leader) {
             ptx::umma_commit(drain);
             ptx::mbar_wait_nocancel(drain, 0, kSpinLimitCycles / 4);
         }
-    } else {
+        if (WIDE) __syncwarp();
+    } else if (warp >= 2) {
         // ------------------------------------------------------------ epilogue
         const int ew = warp - 2;            // 0 .. EPI_WARPS-1
         const int q = warp & 3;             // TMEM lane quarter this warp may access

@@ -64,6 +64,21 @@ __device__ __forceinline__ bool mbar_wait_nocancel(uint64_t* bar, uint32_t parit
     return true;
 }
 
+// One lane of the converged warp (the lowest) is elected.  Code that issues
+// tcgen05 operations from an elected lane of a warp that runs the loop as a
+// whole keeps its descriptor arithmetic warp-uniform; issued from a
+// single-lane branch instead, the UMMA stream slows under integer work on the
+// same SM sub-partition.
+__device__ __forceinline__ bool elect_one() {
+    uint32_t pred;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t.reg .b32 r;\n\t"
+        "elect.sync r|p, 0xffffffff;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(pred));
+    return pred != 0;
+}
+
 // ---- TMA ---------------------------------------------------------------------
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
     asm volatile(

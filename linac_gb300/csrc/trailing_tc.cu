@@ -28,7 +28,8 @@
 // Kernel (tc_kernels.cuh): one CTA per 128-row block and a run of consecutive
 // 32-column tiles (chosen to fill whole waves of the GPU); warp 0 issues the
 // TMA loads (E digits once, B digits through a 4-stage ring), warp 1 issues
-// the UMMAs and owns the TMEM allocation (two accumulators of 7 x 32 columns,
+// the UMMAs (each warp runs its loop as a whole, one elected lane issuing)
+// and owns the TMEM allocation (two accumulators of 7 x 32 columns,
 // so the epilogue of one tile overlaps the UMMAs of the next), warps 2-9
 // (two per TMEM lane quarter, 16 columns each) drain TMEM, re-zero it,
 // combine and write C.

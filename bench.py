@@ -555,10 +555,10 @@ PROFILED_TRAFFIC = {
 
 # 32-bit limb contraction: DRAM bytes per byte of C read and written, from one
 # `--set full` capture of a single 8192 x 8192 x 128 launch (limb_gemm_8192):
-# 501.8 MB of DRAM traffic for 536.9 MB of C (the operand digits add 17 MB;
+# 500.7 MB of DRAM traffic for 536.9 MB of C (the operand digits add 17 MB;
 # the last writes were still in L2 when the kernel ended).  A launch's
 # traffic is this ratio times its 8 m N bytes of C.
-LIMB_U32_TRAFFIC_PER_C_BYTE = 501.8e6 / 536.9e6
+LIMB_U32_TRAFFIC_PER_C_BYTE = 500.7e6 / 536.9e6
 
 
 # loader: DRAM bytes per algorithmic byte of one load_pairs_kernel launch

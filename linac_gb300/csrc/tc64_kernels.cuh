@@ -311,17 +311,41 @@ static __global__ void __launch_bounds__(THREADS, 1)
             ptx::mbar_arrive(&acc_empty[0]);
             ptx::mbar_arrive(&acc_empty[1]);
         }
-        int64_t w[GROUPS];
+        // w_s = wh_s 2^32 + wl_s (wl_s unsigned): T = off + A0 + A1 2^32 with A0 = sum_s y_s wl_s and
+        // A1 = sum_s y_s wh_s, both below 2^59 in magnitude.  The groups enter as b_s = y_s + 0x4B400000
+        // (the bit pattern of the magic-number conversion); the sums of b_s wl_s and b_s wh_s are formed
+        // modulo 2^64 from starting values -0x4B400000 sum wl and -0x4B400000 sum wh, which leaves A0
+        // and A1 exactly (as signed 64-bit values) at the end.
+        // (the weights stay in the kernel's parameter space: operands of the multiply-adds, no registers)
+        uint64_t swl = 0, swh = 0;
 #pragma unroll
-        for (int g = 0; g < GROUPS; ++g) w[g] = P.w[g];
+        for (int g = 0; g < GROUPS; ++g) {
+            swl += (uint32_t)P.w[g];
+            swh += (uint64_t)(int64_t)(int32_t)(P.w[g] >> 32);
+        }
+        const uint64_t a0_init = 0ull - (uint64_t)MAGIC_I * swl;
+        const uint64_t a1_init = 0ull - (uint64_t)MAGIC_I * swh;
         for (int t = 0; t < ntiles; ++t) {
             const int buf = t & 1;
             const int64_t col0 = (int64_t)(t0 + t) * BN + 8 * half;
             uint64_t* crow = P.C + (row_ok ? row : 0) * P.ldc + col0;
             const int ncols = (int)((P.N - col0) < 8 ? (P.N - col0) : 8);
+            const bool vec = row_ok && ncols == 8 && ((((uintptr_t)crow) & 15) == 0);
             uint64_t old[8];
+            if (P.overwrite) {
 #pragma unroll
-            for (int c = 0; c < 8; ++c) old[c] = (row_ok && c < ncols && !P.overwrite) ? crow[c] : 0ull;
+                for (int c = 0; c < 8; ++c) old[c] = 0ull;
+            } else if (vec) {
+#pragma unroll
+                for (int c = 0; c < 8; c += 2) {
+                    const ulonglong2 v = *(const ulonglong2*)(crow + c);
+                    old[c] = v.x;
+                    old[c + 1] = v.y;
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) old[c] = (row_ok && c < ncols) ? crow[c] : 0ull;
+            }
             const bool got = ptx::mbar_wait(&acc_full[buf], (t >> 1) & 1, &s_err);
             if (!__all_sync(0xffffffffu, got)) {
                 if (lane == 0) flag_error64(P, &s_err);
@@ -338,28 +362,35 @@ static __global__ void __launch_bounds__(THREADS, 1)
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&acc_empty[buf]);
+            // groups 0-3 and 11-14 sum at most four digit products per K step (<= 2^22 for K = 64):
+            // the magic-number conversion is exact for them; groups 4-10 are checked
             float mx = 0.f;
 #pragma unroll
-            for (int g = 0; g < GROUPS; ++g)
+            for (int g = 4; g <= 10; ++g)
 #pragma unroll
                 for (int c = 0; c < 8; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
             const bool fast = __all_sync(0xffffffffu, mx <= 4194304.0f);
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
-                // T = sum_g y_g w_g = A0 + A1 2^32 with w_g = wh 2^32 + wl: both parts exact in int64
-                int64_t a0 = 0, a1 = 0;
+                uint64_t a0 = a0_init, a1 = a1_init;  // modulo 2^64
 #pragma unroll
                 for (int g = 0; g < GROUPS; ++g) {
-                    const int32_t y = fast ? (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F)) - MAGIC_I
-                                           : __float2int_rn(__uint_as_float(d[g][c]));
-                    a0 += (int64_t)y * (int64_t)(uint32_t)w[g];
-                    a1 += (int64_t)y * (int64_t)(int32_t)(w[g] >> 32);
+                    const uint32_t b = fast ? __float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F))
+                                            : (uint32_t)(__float2int_rn(__uint_as_float(d[g][c])) + MAGIC_I);
+                    a0 += (uint64_t)b * (uint32_t)P.w[g];
+                    a1 += (uint64_t)((int64_t)b * (int64_t)(int32_t)(P.w[g] >> 32));
                 }
-                // T + off as an unsigned 128-bit (hi:lo)
-                const unsigned __int128 T = (unsigned __int128)((__int128)a0 + ((__int128)a1 << 32)) +
-                                            (((unsigned __int128)P.off_hi << 64) | P.off_lo);
-                const uint64_t v = f.redc((uint64_t)T, (uint64_t)(T >> 64));
-                if (row_ok && c < ncols) crow[c] = f.add(old[c], v);
+                const unsigned __int128 T = (((unsigned __int128)P.off_hi << 64) | P.off_lo) +
+                                            (unsigned __int128)((__int128)(int64_t)a0 + ((__int128)(int64_t)a1 << 32));
+                old[c] = f.add(old[c], f.redc((uint64_t)T, (uint64_t)(T >> 64)));
+                if (c & 1) {  // store each finished pair of columns
+                    if (vec) {
+                        *(ulonglong2*)(crow + c - 1) = make_ulonglong2(old[c - 1], old[c]);
+                    } else if (row_ok) {
+                        if (c - 1 < ncols) crow[c - 1] = old[c - 1];
+                        if (c < ncols) crow[c] = old[c];
+                    }
+                }
             }
         }
     }

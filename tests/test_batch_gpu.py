@@ -32,6 +32,25 @@ def test_batch_uneven_primes_matches_oracle():
         assert pv == piv_ref
 
 
+def test_batch_barrett_primes_match_oracle():
+    """Primes the limb epilogue reduces by Barrett (p = 2 and 2^31 <= p < 2^32) next to
+    Montgomery ones in one plan, with matrices wide enough for several column tiles."""
+    rng = np.random.default_rng(11)
+    specs = [(300, 420, 4294967291), (260, 700, 2147483659), (200, 333, 2), (150, 160, 3221225473),
+             (330, 300, 2**31 - 1)]
+    mats, primes = [], []
+    for m, n, p in specs:
+        r = min(m, n) - 7
+        mats.append(workloads.rank_deficient_modp(m, n, r, p, rng).astype(np.uint32) if p > 2
+                    else rng.integers(0, 2, size=(m, n), dtype=np.uint64).astype(np.uint32))
+        primes.append(p)
+    res, pivs = rref_batch(mats, primes, return_pivots=True, tune=False)
+    for A, p, R, pv in zip(mats, primes, res, pivs):
+        R_ref, piv_ref, _ = oracle.rref_modp(A, p)
+        assert np.array_equal(R.astype(np.uint64), R_ref)
+        assert pv == piv_ref
+
+
 def test_batch_structured_and_edge_matrices():
     rng = np.random.default_rng(5)
     p = 2**31 - 1

@@ -204,9 +204,11 @@ int64_t lnc_batch_plan_bytes(void* plan);
 /* One CUDA graph over `count` plans (a batch cut into chunks): each plan's
  * graph is a child graph, with no dependency between plans, so one launch
  * (lnc_batch_group_run, asynchronous) reduces every chunk and the GPU
- * overlaps them.  The plans must outlive the group; lnc_batch_plan_finish of
- * each plan completes a run.  No counterpart in the reference (see
- * lnc_batch_plan_create). */
+ * overlaps them.  The plans must outlive the group and must not run on their
+ * own while a group run is in flight; once the group's stream has completed
+ * the run (synchronise it, or make each plan's stream wait on it),
+ * lnc_batch_plan_finish of each plan completes the run.  No counterpart in the
+ * reference (see lnc_batch_plan_create). */
 int lnc_batch_group_create(void* const* plans, int64_t count, void** group);
 int lnc_batch_group_run(void* group, void* stream);
 int lnc_batch_group_destroy(void* group);

@@ -171,6 +171,21 @@ __device__ __forceinline__ void flag_error64(const Params64& P, volatile int* ct
 }
 
 // C[rows of block blockIdx.y, tiles [blockIdx.x * TILES_PER_CTA, ...)] += E B (mod p)
+// One output column's group sums: b_g = y_g + 0x4B400000 (the bit pattern of the magic-number
+// conversion, or F2I plus the same constant) times the low and high 32-bit halves of w_g, added
+// modulo 2^64 to the start values a0, a1.
+template <bool FAST>
+__device__ __forceinline__ void group_sums(const uint32_t (&d)[GROUPS][8], int c, const Params64& P, uint64_t& a0,
+                                           uint64_t& a1) {
+#pragma unroll
+    for (int g = 0; g < GROUPS; ++g) {
+        const uint32_t b = FAST ? __float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F))
+                                : (uint32_t)(__float2int_rn(__uint_as_float(d[g][c])) + MAGIC_I);
+        a0 += (uint64_t)b * (uint32_t)P.w[g];
+        a1 += (uint64_t)((int64_t)b * (int64_t)(int32_t)(P.w[g] >> 32));
+    }
+}
+
 static __global__ void __launch_bounds__(THREADS, 1)
     limb64_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                        const __grid_constant__ Params64 P) {
@@ -370,16 +385,8 @@ static __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                 for (int c = 0; c < 8; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
             const bool fast = __all_sync(0xffffffffu, mx <= 4194304.0f);
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                uint64_t a0 = a0_init, a1 = a1_init;  // modulo 2^64
-#pragma unroll
-                for (int g = 0; g < GROUPS; ++g) {
-                    const uint32_t b = fast ? __float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F))
-                                            : (uint32_t)(__float2int_rn(__uint_as_float(d[g][c])) + MAGIC_I);
-                    a0 += (uint64_t)b * (uint32_t)P.w[g];
-                    a1 += (uint64_t)((int64_t)b * (int64_t)(int32_t)(P.w[g] >> 32));
-                }
+            // the rest of an output column once its two partial sums are formed (modulo 2^64)
+            auto finish = [&](int c, uint64_t a0, uint64_t a1) {
                 const unsigned __int128 T = (((unsigned __int128)P.off_hi << 64) | P.off_lo) +
                                             (unsigned __int128)((__int128)(int64_t)a0 + ((__int128)(int64_t)a1 << 32));
                 old[c] = f.add(old[c], f.redc((uint64_t)T, (uint64_t)(T >> 64)));
@@ -390,6 +397,22 @@ static __global__ void __launch_bounds__(THREADS, 1)
                         if (c - 1 < ncols) crow[c - 1] = old[c - 1];
                         if (c < ncols) crow[c] = old[c];
                     }
+                }
+            };
+            // one conversion or the other for the whole warp (a uniform branch, not a select per group)
+            if (fast) {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    uint64_t a0 = a0_init, a1 = a1_init;
+                    group_sums<true>(d, c, P, a0, a1);
+                    finish(c, a0, a1);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    uint64_t a0 = a0_init, a1 = a1_init;
+                    group_sums<false>(d, c, P, a0, a1);
+                    finish(c, a0, a1);
                 }
             }
         }

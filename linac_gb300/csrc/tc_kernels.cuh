@@ -479,15 +479,26 @@ __device__ __forceinline__ void limb_cta(const LimbJob& P, const CUtensorMap* tm
 #pragma unroll
                     for (int c = 0; c < 16; ++c) mx = fmaxf(mx, fabsf(__uint_as_float(d[g][c])));
                 const bool fast = __all_sync(0xffffffffu, mx <= 4194304.0f);
+                // one conversion or the other for the whole warp (a uniform branch, not a select per group)
+                if (fast) {
 #pragma unroll
-                for (int c = 0; c < 16; ++c) {
-                    int32_t y[GROUPS];
+                    for (int c = 0; c < 16; ++c) {
+                        int32_t y[GROUPS];
 #pragma unroll
-                    for (int g = 0; g < GROUPS; ++g)
-                        y[g] = fast ? (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F)) - MAGIC_I
-                                    : __float2int_rn(__uint_as_float(d[g][c]));
-                    const double v = fx_digit_value(y);
-                    if (row_ok && c < ncols) crow[c * estride] = old[c] + (v * rs) * cs[c];
+                        for (int g = 0; g < GROUPS; ++g)
+                            y[g] = (int32_t)__float_as_uint(__fadd_rn(__uint_as_float(d[g][c]), MAGIC_F)) - MAGIC_I;
+                        const double v = fx_digit_value(y);
+                        if (row_ok && c < ncols) crow[c * estride] = old[c] + (v * rs) * cs[c];
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        int32_t y[GROUPS];
+#pragma unroll
+                        for (int g = 0; g < GROUPS; ++g) y[g] = __float2int_rn(__uint_as_float(d[g][c]));
+                        const double v = fx_digit_value(y);
+                        if (row_ok && c < ncols) crow[c * estride] = old[c] + (v * rs) * cs[c];
+                    }
                 }
             }
         } else {

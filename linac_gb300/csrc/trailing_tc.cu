@@ -15,7 +15,7 @@
 //    every FP32 accumulation in TMEM is an exact integer;
 //  * the epilogue converts the seven group sums D_s to integers (x + 1.5 2^23
 //    where |x| <= 2^22, F2I otherwise), forms sum_s D_s (256^s mod p) in
-//    64-bit (groups (0, 1) and (5, 6) paired first by a shift-add), reduces
+//    64-bit (groups (0, 1), (2, 3) and (5, 6) paired first by a shift-add), reduces
 //    it mod p (one Montgomery step for odd p < 2^31, the weights carrying the
 //    factor 2^32; Barrett otherwise) and adds it to the old residue.
 //
